@@ -1,0 +1,89 @@
+/* CPU oracle for the EDXRaster rasterization pipeline (test infrastructure).
+ *
+ * A plain-C restatement of Renderer::RenderMesh (EDXRaster/Core/Renderer.cpp:
+ * 100-118) for one frame: vertex transform, homogeneous clipping, fixed-point
+ * triangle setup, 32x32 binning, coarse/fine/trivial-accept rasterization,
+ * the depth test, and "last passing fragment wins" colour resolve.  Integer,
+ * ordering and depth results are bit-exact with the reference; colour is an
+ * FP64 evaluation of the shading model at the winning fragment.
+ *
+ * Only tests, the smoke check and the benchmark's CPU-baseline leg use this
+ * code, and only as the checker.  The product library never links it.
+ */
+#ifndef EDXR_ORACLE_H
+#define EDXR_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum
+{
+    EDXR_ORACLE_DEPTH_LEQUAL = 0, /* FrameBuffer.cpp:64 (reference) */
+    EDXR_ORACLE_DEPTH_LESS = 1
+};
+
+enum
+{
+    EDXR_ORACLE_PS_BLINN_PHONG = 0,           /* albedo*diffuse + ks*max(N.H,0)^s */
+    EDXR_ORACLE_PS_BLINN_PHONG_REFERENCE = 1, /* Shader.h:249-281: diffuse + ks*(N.H)^s */
+    EDXR_ORACLE_PS_LAMBERTIAN_ALBEDO = 2,     /* Shader.h:212-243 with per-vertex albedo */
+    EDXR_ORACLE_PS_LAMBERTIAN = 3             /* Shader.h:188-206 */
+};
+
+typedef struct
+{
+    int width, height;
+    float mv[16];     /* row-major, column vectors */
+    float proj[16];
+    float raster[16];
+    int depth_func;   /* EDXR_ORACLE_DEPTH_* */
+    int hierarchical; /* RenderStates::HierarchicalRasterize */
+    int shader;       /* EDXR_ORACLE_PS_* */
+    float light[3];   /* direction towards the light, normalised inside */
+    float ks, shininess;
+    int threads;      /* worker threads for the per-tile stages (>=1) */
+} edxr_oracle_params;
+
+typedef struct
+{
+    const float* positions; int position_stride; /* strides in floats */
+    const float* normals;   int normal_stride;   /* may be NULL -> 0 */
+    const float* uvs;       int uv_stride;       /* may be NULL -> 0 */
+    const float* albedo;    int albedo_stride;   /* may be NULL -> 1 */
+    const uint32_t* indices;                     /* 3 per triangle */
+    int nv, nt;
+} edxr_oracle_mesh;
+
+typedef struct
+{
+    uint32_t* id;     /* W*H input-triangle index of the winner, 0xFFFFFFFF if none */
+    float* depth;     /* W*H final depth buffer (clear value 1.0) */
+    float* lambda0;   /* W*H winner barycentrics (optional) */
+    float* lambda1;
+    double* color;    /* W*H*4 RGBA, alpha 1 where covered (optional) */
+    /* statistics */
+    long long fragments;   /* quad fragments emitted */
+    long long raster_tris; /* triangles that survived setup */
+    long long clipped_input_tris;
+    long long bin_refs;
+} edxr_oracle_out;
+
+/* Returns 0 on success, negative on invalid arguments or allocation failure. */
+int edxr_oracle_render(const edxr_oracle_params* params, const edxr_oracle_mesh* mesh,
+                       edxr_oracle_out* out);
+
+/* FP64 evaluation of the shading model at an arbitrary point, exposed so the
+ * adjoint tests can difference it.  Inputs are the per-vertex attributes of
+ * one triangle, its perspective-correct barycentrics and the eye position. */
+void edxr_oracle_shade(const edxr_oracle_params* params, const double b[3],
+                       const double pos[3][3], const double nrm[3][3],
+                       const double alb[3][3], const double eye[3], double rgb[3]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
