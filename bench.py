@@ -1,0 +1,345 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 rasterization pipeline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload terrain|sphere|stress]
+    python bench.py --impl reference ...
+
+A step is one frame of the workload: Renderer::RenderMesh semantics (clear,
+vertex transform, clipping, setup, binning, rasterization, shading, depth
+test) over one synthetic mesh.  The default workload is the heightfield
+terrain (1024x1024 quads = 2,097,152 triangles at 1920x1080), the
+configuration the throughput metric is quoted on.
+
+Printed JSON (one line, rank 0):
+  value       input triangles per second (Mtris/s), inputs resident in HBM,
+              device time of K frames from CUDA events on the renderer's
+              stream, L2 flushed (a 512 MiB write) before every frame;
+  e2e         the same metric through the public API with pinned host
+              buffers: mesh upload, render and read-back of colour, depth and
+              triangle ids inside the timed region (wall clock);
+  roofline    HBM roofline of the dominant kernel (k_raster, stage events);
+  cpu_baseline the CPU restatement of the reference pipeline (oracle port)
+              on this host's cores, one full frame.
+With --impl reference the CPU implementation of the reference pipeline is
+timed instead (the reference's own sources compiled against the shim when
+they are present here, else the oracle port).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from edxraster_gb300 import scenes  # noqa: E402
+
+WORKLOADS = {
+    "terrain": ("heightfield 1024x1024 quads (2,097,152 tris) at 1920x1080, low camera, Blinn-Phong, depth LESS",
+                lambda: scenes.terrain_scene(1024, 1920, 1080, seed=1)),
+    "sphere": ("UV sphere 32x64 (4,032 tris) at 1280x720, Blinn-Phong ks 0.5 shininess 32, depth LESS",
+               lambda: scenes.sphere_scene(1280, 720, seed=0)),
+    "stress": ("binning stress: 1,000,000 clip-space tris, log-uniform areas 0.1-1e4 px, at 3840x2160, depth LESS",
+               lambda: scenes.stress_scene(1_000_000, 3840, 2160, seed=7)),
+}
+PIXEL_BYTES = 24  # RGBA32F colour + D32F depth + u32 triangle id per pixel
+
+
+def mesh_bytes(mesh) -> int:
+    # compulsory input: position, normal, albedo per vertex, 3 indices per triangle
+    return mesh.nv * 36 + mesh.nt * 12
+
+
+def algorithmic_bytes(sc) -> int:
+    return mesh_bytes(sc.mesh) + sc.view.width * sc.view.height * PIXEL_BYTES
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profiles(workload):
+    """DRAM bytes per k_raster launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "k_raster_%s.md" % workload)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(float(line.split(":", 1)[1].strip()))
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi SM clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_oracle_time(sc, threads: int):
+    from oracle import pyoracle
+    t0 = time.perf_counter()
+    pyoracle.render_oracle(sc.mesh, sc.view, threads=threads, with_color=True)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(sc, frames: int = 1):
+    """The oracle port on this host: best of `frames` full frames."""
+    threads = os.cpu_count() or 1
+    times = [cpu_oracle_time(sc, threads) for _ in range(max(1, frames))]
+    t = min(times)
+    return {"value": sc.mesh.nt / t / 1e6, "unit": "Mtris/s", "cores": threads, "kind": "port",
+            "sample": "one full frame of the workload (%d tris, %dx%d) per measurement, best of %d"
+                      % (sc.mesh.nt, sc.view.width, sc.view.height, len(times))}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    name, make = WORKLOADS[args.workload]
+    sc = make()
+    kind = "port"
+    t_frames = []
+    cores = os.cpu_count() or 1
+    from oracle import pyoracle
+    use_ref = pyoracle.reference_lib() is not None
+    if use_ref:
+        kind = "reference"
+        t, cores = pyoracle.time_reference(sc.mesh, sc.view, frames=args.steps, warmup=args.warmup)
+        t_frames = [t]
+    else:
+        for i in range(args.warmup + args.steps):
+            dt = cpu_oracle_time(sc, cores)
+            if i >= args.warmup:
+                t_frames.append(dt)
+    t = statistics.median(t_frames)
+    value = sc.mesh.nt / t / 1e6
+    sample = ("Renderer::RenderMesh of the reference (its Core sources built against oracle/shim), "
+              "median of %d frames" % args.steps) if use_ref else \
+        ("CPU restatement of the reference pipeline (oracle/edxr_oracle.c), median of %d full frames" % args.steps)
+    line = {
+        "impl": "reference", "metric": "Mtris/s", "value": value, "unit": "Mtris/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic",
+        "config": {"workload": args.workload, "description": name, "triangles": sc.mesh.nt,
+                   "width": sc.view.width, "height": sc.view.height},
+        "gpix_per_s": sc.view.width * sc.view.height / t / 1e9, "fps": 1.0 / t,
+        "cpu_baseline": {"value": value, "unit": "Mtris/s", "cores": cores, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+    from edxraster_gb300 import renderer as R
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    name, make = WORKLOADS[args.workload]
+    sc = make()
+    W, H = sc.view.width, sc.view.height
+    stream = torch.cuda.Stream()
+    r = R.Renderer(device=local, stream=stream)
+    r.Initialize(W, H)
+    R.configure(r, sc.view)
+    dmesh = R.DeviceMesh.from_mesh(sc.mesh, device="cuda:%d" % local)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:%d" % local)
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    # ---- device-resident throughput ------------------------------------
+    for _ in range(args.warmup):
+        flush_l2()
+        r.RenderMesh(dmesh, synchronize=False)
+    r.Synchronize()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    for i in range(args.steps):
+        flush_l2()
+        starts[i].record(stream)
+        r.RenderMesh(dmesh, synchronize=False)
+        ends[i].record(stream)
+    r.Synchronize()
+    torch.cuda.synchronize()
+    clock_info = clocks.stop()
+    per = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(per)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda:%d" % local)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    stats = r.Stats()
+    ms_per_step = total_ms / args.steps
+    value = world * sc.mesh.nt * args.steps / (total_ms / 1e3) / 1e6
+
+    # ---- stage times (dominant kernel) ---------------------------------
+    r.SetProfiling(True)
+    stage_sum = {}
+    for i in range(args.warmup + args.steps):
+        flush_l2()
+        r.RenderMesh(dmesh, synchronize=True)
+        if i >= args.warmup:
+            for k, v in r.StageTimes().items():
+                stage_sum[k] = stage_sum.get(k, 0.0) + v
+    r.SetProfiling(False)
+    stage_ms = {k: v / args.steps for k, v in stage_sum.items()}
+    raster_ms = stage_ms.get("raster+shade", float("nan"))
+    peak, peak_kind = load_peaks()
+    raster_bytes = W * H * PIXEL_BYTES
+    achieved = raster_bytes / (raster_ms / 1e3) / 1e9
+    frame_achieved = algorithmic_bytes(sc) / (ms_per_step / 1e3) / 1e9
+
+    # ---- end to end through the public API with host buffers -----------
+    hmesh = R.HostMesh(sc.mesh, pinned=True)
+    color = torch.empty((H, W, 4), dtype=torch.float32).pin_memory().numpy()
+    depth = torch.empty((H, W), dtype=torch.float32).pin_memory().numpy()
+    tid = torch.empty((H, W), dtype=torch.int32).pin_memory().numpy()
+    lib = r._lib
+
+    def e2e_step():
+        r.RenderMesh(hmesh, synchronize=False)
+        R._lib.check(lib.edxr_read_outputs(r._h, color.ctypes.data, depth.ctypes.data, tid.ctypes.data))
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * sc.mesh.nt * args.steps / e2e_s / 1e6
+    r.close()
+
+    if rank != 0:
+        return 0
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(sc)
+    traffic = traffic_from_profiles(args.workload)
+    line = {
+        "metric": "Mtris/s", "value": value, "unit": "Mtris/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic (seeded scene generators)",
+        "config": {"workload": args.workload, "description": name, "triangles": sc.mesh.nt, "width": W,
+                   "height": H, "l2": "512 MiB write between timed frames",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "gpix_per_s": world * W * H / (ms_per_step / 1e3) / 1e9,
+        "fps": world * 1e3 / ms_per_step,
+        "stage_ms": stage_ms,
+        "frame_roofline": {"algorithmic_bytes": algorithmic_bytes(sc), "achieved_gbs": frame_achieved,
+                           "frac": frame_achieved / peak},
+        "roofline": {"kernel": "k_raster", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": raster_bytes, "launch_ms": raster_ms},
+        "e2e": {"value": e2e_value, "unit": "Mtris/s", "h2d_bytes_per_step": hmesh.nbytes(),
+                "d2h_bytes_per_step": W * H * PIXEL_BYTES},
+        "gpu_launches": int(stats.kernels_per_pass) * args.steps,
+        "clocks": clock_info,
+        "raster_triangles": int(stats.raster_triangles), "bin_entries": int(stats.bin_entries),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="terrain", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_gpu(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,847 @@
+// C ABI of the EDXRaster GB300 pipeline (include/edxr.h): renderer object,
+// device buffers, per-frame descriptors, overflow recovery and CUDA-graph
+// replay of the kernel sequence.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "edxr.h"
+#include "edxr_internal.h"
+
+using namespace edxr;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+edxr_status fail(edxr_status s, const std::string& msg)
+{
+    g_last_error = msg;
+    return s;
+}
+
+#define EDXR_CUDA(call)                                                                        \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(e_ == cudaErrorMemoryAllocation ? EDXR_ERR_OUT_OF_MEMORY : EDXR_ERR_CUDA, \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+    } while (0)
+
+// Grow-only device allocation.
+struct DevBuf
+{
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need)
+    {
+        if (need <= bytes)
+            return cudaSuccess;
+        if (ptr)
+            cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&ptr, need);
+        if (e == cudaSuccess)
+            bytes = need;
+        return e;
+    }
+    void release()
+    {
+        if (ptr)
+            cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <typename T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+void mat_mul(const float* A, const float* B, float* C)
+{
+    // P * MV as Renderer.cpp:90, each entry summed left to right in float
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
+        {
+            float s = A[i * 4] * B[j];
+            s = s + A[i * 4 + 1] * B[4 + j];
+            s = s + A[i * 4 + 2] * B[8 + j];
+            s = s + A[i * 4 + 3] * B[12 + j];
+            C[i * 4 + j] = s;
+        }
+}
+
+// Eye position MV^-1 * 0 (Renderer.cpp:289) by Gauss-Jordan in double.
+bool eye_from_mv(const float* mv, float eye[3])
+{
+    double a[4][8];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
+        {
+            a[i][j] = mv[i * 4 + j];
+            a[i][j + 4] = i == j ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 4; c++)
+    {
+        int piv = c;
+        for (int r = c + 1; r < 4; r++)
+            if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+        if (a[piv][c] == 0.0)
+            return false;
+        if (piv != c)
+            for (int j = 0; j < 8; j++) std::swap(a[c][j], a[piv][j]);
+        const double d = a[c][c];
+        for (int j = 0; j < 8; j++) a[c][j] /= d;
+        for (int r = 0; r < 4; r++)
+        {
+            if (r == c) continue;
+            const double m = a[r][c];
+            for (int j = 0; j < 8; j++) a[r][j] -= m * a[c][j];
+        }
+    }
+    const double w = a[3][7];
+    eye[0] = (float)(a[0][7] / w);
+    eye[1] = (float)(a[1][7] / w);
+    eye[2] = (float)(a[2][7] / w);
+    return true;
+}
+
+struct Camera
+{
+    float mv[16], proj[16], raster[16];
+    bool set = false;
+};
+
+struct Shading
+{
+    int ps_kind = EDXR_PS_BLINN_PHONG;
+    edxr_shader_params p = { { 1.0f, 1.0f, -1.0f }, 0.5f, 32.0f };
+};
+
+struct MeshStage
+{
+    DevBuf pos, nrm, alb, uv, idx;
+};
+
+}  // namespace
+
+struct edxr_renderer
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+    uint32_t width = 0, height = 0;
+    edxr_state state = { EDXR_DEPTH_LEQUAL, 1, 0, 0 };
+    Shading shading;
+    Camera cam;
+
+    DevBuf frames, clip, rtris, polys, tile_count, tile_offset, tile_cursor, bins, big_list, counters, status;
+    DevBuf color, depth, tri_id, back8;
+    uint64_t bin_capacity = 0, rtri_cap = 0, poly_cap = 0, big_cap = 0;
+    std::vector<MeshStage> stage;
+    FrameDesc* frames_host = nullptr;  // pinned
+    size_t frames_host_cap = 0;
+    DeviceStatus* status_host = nullptr;  // pinned
+    cudaEvent_t done = nullptr;
+
+    // the last pass, for synchronize / overflow recovery
+    PassArgs last = {};
+    bool pending = false;
+    uint32_t last_frames = 0, out_width = 0, out_height = 0;
+    uint32_t rerenders = 0;
+    std::vector<uint8_t> back_host;
+
+    // CUDA graph of the kernel sequence, replayed while the pass layout is unchanged
+    bool use_graphs = true;
+    cudaGraphExec_t graph = nullptr;
+    PassArgs graph_args = {};
+
+    // stage timing
+    bool profiling = false;
+    cudaEvent_t stage_ev[kStageEvents] = {};
+};
+
+namespace {
+
+bool same_args(const PassArgs& a, const PassArgs& b) { return std::memcmp(&a, &b, sizeof(PassArgs)) == 0; }
+
+cudaError_t run_pass(edxr_renderer* r, const PassArgs& a)
+{
+    if (r->profiling)
+        return launch_pipeline(a, r->stream, r->stage_ev);
+    if (!r->use_graphs || r->stream == nullptr)
+        return launch_pipeline(a, r->stream);
+    if (r->graph && same_args(a, r->graph_args))
+        return cudaGraphLaunch(r->graph, r->stream);
+    if (r->graph)
+    {
+        cudaGraphExecDestroy(r->graph);
+        r->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess)
+        return launch_pipeline(a, r->stream);
+    cudaError_t le = launch_pipeline(a, r->stream);
+    e = cudaStreamEndCapture(r->stream, &g);
+    if (le != cudaSuccess || e != cudaSuccess)
+    {
+        if (g) cudaGraphDestroy(g);
+        return le != cudaSuccess ? le : e;
+    }
+    e = cudaGraphInstantiate(&r->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+    {
+        r->graph = nullptr;
+        return launch_pipeline(a, r->stream);
+    }
+    r->graph_args = a;
+    return cudaGraphLaunch(r->graph, r->stream);
+}
+
+edxr_status check_mesh(const edxr_mesh* m)
+{
+    if (!m)
+        return fail(EDXR_ERR_INVALID_ARG, "mesh is NULL");
+    if (m->num_triangles > 0 && (!m->positions || !m->indices))
+        return fail(EDXR_ERR_INVALID_ARG, "mesh positions and indices are required");
+    if (m->num_triangles >= (1u << 28))
+        return fail(EDXR_ERR_INVALID_ARG, "more than 2^28 triangles in one mesh");
+    if (m->memory != EDXR_MEMORY_HOST && m->memory != EDXR_MEMORY_DEVICE)
+        return fail(EDXR_ERR_INVALID_ARG, "mesh memory must be EDXR_MEMORY_HOST or EDXR_MEMORY_DEVICE");
+    if (m->positions && m->position_stride < 12)
+        return fail(EDXR_ERR_INVALID_ARG, "position stride below 12 bytes");
+    if (m->normals && m->normal_stride < 12)
+        return fail(EDXR_ERR_INVALID_ARG, "normal stride below 12 bytes");
+    if (m->albedo && m->albedo_stride < 12)
+        return fail(EDXR_ERR_INVALID_ARG, "albedo stride below 12 bytes");
+    if (m->uvs && m->uv_stride < 8)
+        return fail(EDXR_ERR_INVALID_ARG, "uv stride below 8 bytes");
+    if (m->memory == EDXR_MEMORY_HOST)
+    {
+        // the reference asserts on index range (InputBuffer.h:177); check here
+        const uint64_t n = 3ull * m->num_triangles;
+        for (uint64_t i = 0; i < n; i++)
+            if (m->indices[i] >= m->num_vertices)
+                return fail(EDXR_ERR_INVALID_ARG, "vertex index out of range");
+    }
+    return EDXR_OK;
+}
+
+// Copy a host mesh to device staging buffers; returns a device-memory mesh.
+edxr_status stage_mesh(edxr_renderer* r, size_t slot, const edxr_mesh* in, edxr_mesh* out)
+{
+    *out = *in;
+    if (in->memory == EDXR_MEMORY_DEVICE)
+        return EDXR_OK;
+    if (r->stage.size() <= slot)
+        r->stage.resize(slot + 1);
+    MeshStage& s = r->stage[slot];
+    const size_t nv = in->num_vertices;
+    auto copy = [&](DevBuf& buf, const void* src, uint32_t stride, size_t elem, const void** dst, uint32_t* dst_stride) -> edxr_status {
+        if (!src)
+            return EDXR_OK;
+        EDXR_CUDA(buf.ensure(nv * stride > 0 ? nv * stride : 16));
+        if (nv)
+            EDXR_CUDA(cudaMemcpyAsync(buf.ptr, src, (nv - 1) * (size_t)stride + elem, cudaMemcpyHostToDevice, r->stream));
+        *dst = buf.ptr;
+        *dst_stride = stride;
+        return EDXR_OK;
+    };
+    edxr_status st;
+    if ((st = copy(s.pos, in->positions, in->position_stride, 12, &out->positions, &out->position_stride))) return st;
+    if ((st = copy(s.nrm, in->normals, in->normal_stride, 12, &out->normals, &out->normal_stride))) return st;
+    if ((st = copy(s.alb, in->albedo, in->albedo_stride, 12, &out->albedo, &out->albedo_stride))) return st;
+    if ((st = copy(s.uv, in->uvs, in->uv_stride, 8, &out->uvs, &out->uv_stride))) return st;
+    const size_t ib = 12ull * in->num_triangles;
+    EDXR_CUDA(s.idx.ensure(ib > 0 ? ib : 16));
+    if (ib)
+        EDXR_CUDA(cudaMemcpyAsync(s.idx.ptr, in->indices, ib, cudaMemcpyHostToDevice, r->stream));
+    out->indices = s.idx.as<uint32_t>();
+    out->memory = EDXR_MEMORY_DEVICE;
+    return EDXR_OK;
+}
+
+void fill_frame(FrameDesc& f, const edxr_mesh& m, const Camera& cam, const Shading& sh, int depth_func,
+                int hierarchical, uint32_t width, uint32_t height)
+{
+    std::memset(&f, 0, sizeof(f));
+    f.positions = static_cast<const char*>(m.positions);
+    f.normals = static_cast<const char*>(m.normals);
+    f.albedo = static_cast<const char*>(m.albedo);
+    f.uvs = static_cast<const char*>(m.uvs);
+    f.indices = m.indices;
+    f.pos_stride = m.position_stride;
+    f.nrm_stride = m.normal_stride;
+    f.alb_stride = m.albedo_stride;
+    f.uv_stride = m.uv_stride;
+    f.nv = m.num_vertices;
+    f.nt = m.num_triangles;
+    f.width = (int)width;
+    f.height = (int)height;
+    f.tdx = (int)((width + kTileSize - 1) >> kTileLog2);
+    f.tdy = (int)((height + kTileSize - 1) >> kTileLog2);
+    f.tdx32 = (int)((width + 31) >> 5);
+    f.tdy32 = (int)((height + 31) >> 5);
+    f.ps_kind = sh.ps_kind;
+    f.depth_func = depth_func;
+    f.hierarchical = hierarchical ? 1 : 0;
+    mat_mul(cam.proj, cam.mv, f.mvp);
+    std::memcpy(f.raster, cam.raster, sizeof(f.raster));
+    if (!eye_from_mv(cam.mv, f.eye))
+        f.eye[0] = f.eye[1] = f.eye[2] = 0.0f;
+    const double lx = sh.p.light[0], ly = sh.p.light[1], lz = sh.p.light[2];
+    const double ln = std::sqrt(lx * lx + ly * ly + lz * lz);
+    f.light[0] = (float)(lx / ln);
+    f.light[1] = (float)(ly / ln);
+    f.light[2] = (float)(lz / ln);
+    f.ks = sh.p.ks;
+    f.shininess = sh.p.shininess;
+    // 2D affine inverse of the raster matrix's x/y rows
+    const double a = cam.raster[0], b = cam.raster[1], c = cam.raster[3];
+    const double d = cam.raster[4], e = cam.raster[5], g = cam.raster[7];
+    const double det = a * e - b * d;
+    if (det != 0.0)
+    {
+        f.ndc_from_raster[0] = (float)(e / det);
+        f.ndc_from_raster[1] = (float)(-b / det);
+        f.ndc_from_raster[2] = (float)((b * g - e * c) / det);
+        f.ndc_from_raster[3] = (float)(-d / det);
+        f.ndc_from_raster[4] = (float)(a / det);
+        f.ndc_from_raster[5] = (float)((d * c - a * g) / det);
+    }
+}
+
+// Build the pass over `n` frames (already in r->frames_host) and launch it.
+edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t height)
+{
+    uint64_t tv = 0, tt = 0, tiles = 0;
+    for (uint32_t i = 0; i < n; i++)
+    {
+        FrameDesc& f = r->frames_host[i];
+        f.vtx_base = (uint32_t)tv;
+        f.tri_base = (uint32_t)tt;
+        f.tile_base = (uint32_t)tiles;
+        f.pix_base = (uint64_t)i * width * height;
+        tv += f.nv;
+        tt += f.nt;
+        tiles += (uint64_t)f.tdx * f.tdy;
+    }
+    if (tv >= (1ull << 31) || tt >= (1ull << 28) || tiles >= (1ull << 24))
+        return fail(EDXR_ERR_OVERFLOW, "pass too large: reduce the number of frames per call");
+    const uint64_t pixels = (uint64_t)n * width * height;
+    // Intermediate capacities start from typical needs and grow when a frame
+    // reports an overflow (sync_pass renders that frame again).
+    r->rtri_cap = std::max<uint64_t>({ r->rtri_cap, tt + std::max<uint64_t>(tt / 4, 65536) });
+    r->poly_cap = std::max<uint64_t>({ r->poly_cap, std::max<uint64_t>(tt / 16, 65536) });
+    r->big_cap = std::max<uint64_t>({ r->big_cap, std::max<uint64_t>(tt / 8, 65536) });
+    r->rtri_cap = std::min<uint64_t>(r->rtri_cap, 0xFFFFFFF0u);
+    const uint64_t rcap = r->rtri_cap, pcap = r->poly_cap;
+    const uint64_t nscan = (tiles + 4095) / 4096;
+    if (r->bin_capacity < 2 * tt + 4 * tiles)
+        r->bin_capacity = std::max<uint64_t>(2 * tt + 4 * tiles, 1u << 20);
+    EDXR_CUDA(r->frames.ensure(sizeof(FrameDesc) * n));
+    EDXR_CUDA(r->clip.ensure(sizeof(float4) * std::max<uint64_t>(tv, 1)));
+    EDXR_CUDA(r->rtris.ensure(sizeof(RTri) * rcap));
+    EDXR_CUDA(r->polys.ensure(sizeof(ClipPoly) * pcap));
+    EDXR_CUDA(r->tile_count.ensure(4 * (tiles + 1)));
+    EDXR_CUDA(r->tile_offset.ensure(4 * (tiles + 1)));
+    EDXR_CUDA(r->tile_cursor.ensure(4 * (tiles + 1 + nscan + 1)));
+    EDXR_CUDA(r->bins.ensure(4 * r->bin_capacity));
+    EDXR_CUDA(r->big_list.ensure(4 * r->big_cap));
+    EDXR_CUDA(r->counters.ensure(4 * 8));
+    EDXR_CUDA(r->status.ensure(sizeof(DeviceStatus)));
+    EDXR_CUDA(r->color.ensure(16 * std::max<uint64_t>(pixels, 1)));
+    EDXR_CUDA(r->depth.ensure(4 * std::max<uint64_t>(pixels, 1)));
+    EDXR_CUDA(r->tri_id.ensure(4 * std::max<uint64_t>(pixels, 1)));
+
+    EDXR_CUDA(cudaMemcpyAsync(r->frames.ptr, r->frames_host, sizeof(FrameDesc) * n, cudaMemcpyHostToDevice, r->stream));
+
+    PassArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.frames = r->frames.as<FrameDesc>();
+    a.num_frames = n;
+    a.total_vertices = (uint32_t)tv;
+    a.total_tris = (uint32_t)tt;
+    a.total_tiles = (uint32_t)tiles;
+    a.clip = r->clip.as<float4>();
+    a.rtris = r->rtris.as<RTri>();
+    a.rtri_capacity = (uint32_t)std::min<uint64_t>(rcap, 0xFFFFFFFFu);
+    a.polys = r->polys.as<ClipPoly>();
+    a.poly_capacity = (uint32_t)pcap;
+    a.tile_count = r->tile_count.as<uint32_t>();
+    a.tile_offset = r->tile_offset.as<uint32_t>();
+    a.tile_cursor = r->tile_cursor.as<uint32_t>();
+    a.bins = r->bins.as<uint32_t>();
+    a.bin_capacity = r->bin_capacity;
+    a.big_list = r->big_list.as<uint32_t>();
+    a.big_capacity = (uint32_t)r->big_cap;
+    a.counters = r->counters.as<uint32_t>();
+    a.status = r->status.as<DeviceStatus>();
+    a.color = r->color.as<float4>();
+    a.depth = r->depth.as<float>();
+    a.tri_id = r->tri_id.as<uint32_t>();
+    a.num_sms = r->num_sms;
+
+    EDXR_CUDA(run_pass(r, a));
+    EDXR_CUDA(cudaMemcpyAsync(r->status_host, r->status.ptr, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, r->stream));
+    EDXR_CUDA(cudaEventRecord(r->done, r->stream));
+    r->last = a;
+    r->pending = true;
+    r->last_frames = n;
+    r->out_width = width;
+    r->out_height = height;
+    return EDXR_OK;
+}
+
+edxr_status ensure_frames_host(edxr_renderer* r, size_t n)
+{
+    if (n <= r->frames_host_cap)
+        return EDXR_OK;
+    if (r->frames_host)
+    {
+        cudaEventSynchronize(r->done);
+        cudaFreeHost(r->frames_host);
+        r->frames_host = nullptr;
+        r->frames_host_cap = 0;
+    }
+    EDXR_CUDA(cudaMallocHost((void**)&r->frames_host, sizeof(FrameDesc) * n));
+    r->frames_host_cap = n;
+    return EDXR_OK;
+}
+
+edxr_status sync_pass(edxr_renderer* r)
+{
+    if (!r->pending)
+        return EDXR_OK;
+    for (int attempt = 0;; attempt++)
+    {
+        EDXR_CUDA(cudaEventSynchronize(r->done));
+        EDXR_CUDA(cudaGetLastError());
+        const DeviceStatus st = *r->status_host;
+        if (st.error)
+        {
+            r->pending = false;
+            return fail((edxr_status)st.error, "device reported an error");
+        }
+        if (!st.overflow)
+            break;
+        if (attempt >= 4)
+        {
+            r->pending = false;
+            return fail(EDXR_ERR_OVERFLOW, "intermediate buffer overflow persists after growing");
+        }
+        // grow what overflowed to what the frame needs and render it again
+        PassArgs a = r->last;
+        if (st.overflow & 2u)
+        {
+            r->rtri_cap = std::min<uint64_t>((uint64_t)st.raster_tris + st.raster_tris / 4 + 1024, 0xFFFFFFF0u);
+            EDXR_CUDA(r->rtris.ensure(sizeof(RTri) * r->rtri_cap));
+            a.rtris = r->rtris.as<RTri>();
+            a.rtri_capacity = (uint32_t)r->rtri_cap;
+        }
+        if (st.overflow & 4u)
+        {
+            r->poly_cap = (uint64_t)st.clipped_polys + st.clipped_polys / 4 + 1024;
+            EDXR_CUDA(r->polys.ensure(sizeof(ClipPoly) * r->poly_cap));
+            a.polys = r->polys.as<ClipPoly>();
+            a.poly_capacity = (uint32_t)r->poly_cap;
+        }
+        if (st.overflow & 8u)
+        {
+            r->big_cap = (uint64_t)st.big_tris + st.big_tris / 4 + 1024;
+            EDXR_CUDA(r->big_list.ensure(4 * r->big_cap));
+            a.big_list = r->big_list.as<uint32_t>();
+            a.big_capacity = (uint32_t)r->big_cap;
+        }
+        if (st.overflow & 1u)
+        {
+            // bins are sized from the triangles that were binned; after a
+            // raster-triangle overflow the count is not final, so retry as well
+            r->bin_capacity = st.bins_needed + st.bins_needed / 4 + 1024;
+            EDXR_CUDA(r->bins.ensure(4 * r->bin_capacity));
+            a.bins = r->bins.as<uint32_t>();
+            a.bin_capacity = r->bin_capacity;
+        }
+        r->rerenders++;
+        EDXR_CUDA(run_pass(r, a));
+        EDXR_CUDA(cudaMemcpyAsync(r->status_host, r->status.ptr, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, r->stream));
+        EDXR_CUDA(cudaEventRecord(r->done, r->stream));
+        r->last = a;
+    }
+    r->pending = false;
+    return EDXR_OK;
+}
+
+struct DeviceGuard
+{
+    int prev = -1;
+    explicit DeviceGuard(int d)
+    {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != d)
+            cudaSetDevice(d);
+        else
+            prev = -1;
+    }
+    ~DeviceGuard()
+    {
+        if (prev >= 0)
+            cudaSetDevice(prev);
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* edxr_last_error_string(void) { return g_last_error.c_str(); }
+
+edxr_status edxr_create(edxr_renderer** out, const edxr_init* init)
+{
+    if (!out || !init)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    if (init->width == 0 || init->height == 0 || init->width > 32768 || init->height > 32768)
+        return fail(EDXR_ERR_INVALID_ARG, "framebuffer size must be in [1, 32768]");
+    int ndev = 0;
+    EDXR_CUDA(cudaGetDeviceCount(&ndev));
+    if (init->device < 0 || init->device >= ndev)
+        return fail(EDXR_ERR_INVALID_ARG, "no such CUDA device");
+    DeviceGuard g(init->device);
+    edxr_renderer* r = new edxr_renderer();
+    r->device = init->device;
+    r->stream = static_cast<cudaStream_t>(init->stream);
+    r->width = init->width;
+    r->height = init->height;
+    cudaDeviceGetAttribute(&r->num_sms, cudaDevAttrMultiProcessorCount, r->device);
+    prepare_kernels();  // occupancy queries happen outside any graph capture
+    if (const char* e = std::getenv("EDXR_NO_GRAPHS"))
+        r->use_graphs = e[0] == '0';
+    cudaError_t e = cudaMallocHost((void**)&r->status_host, sizeof(DeviceStatus));
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming);
+    if (e != cudaSuccess)
+    {
+        edxr_destroy(r);
+        return fail(EDXR_ERR_CUDA, std::string("renderer setup: ") + cudaGetErrorString(e));
+    }
+    std::memset(r->status_host, 0, sizeof(DeviceStatus));
+    *out = r;
+    return EDXR_OK;
+}
+
+edxr_status edxr_destroy(edxr_renderer* r)
+{
+    if (!r)
+        return EDXR_OK;
+    DeviceGuard g(r->device);
+    if (r->done)
+        cudaEventSynchronize(r->done);
+    if (r->graph)
+        cudaGraphExecDestroy(r->graph);
+    DevBuf* bufs[] = { &r->frames, &r->clip, &r->rtris, &r->polys, &r->tile_count, &r->tile_offset,
+                       &r->tile_cursor, &r->bins, &r->big_list, &r->counters, &r->status, &r->color,
+                       &r->depth, &r->tri_id, &r->back8 };
+    for (DevBuf* b : bufs)
+        b->release();
+    for (auto& s : r->stage)
+    {
+        s.pos.release(); s.nrm.release(); s.alb.release(); s.uv.release(); s.idx.release();
+    }
+    if (r->frames_host)
+        cudaFreeHost(r->frames_host);
+    if (r->status_host)
+        cudaFreeHost(r->status_host);
+    if (r->done)
+        cudaEventDestroy(r->done);
+    for (int i = 0; i < kStageEvents; i++)
+        if (r->stage_ev[i])
+            cudaEventDestroy(r->stage_ev[i]);
+    delete r;
+    return EDXR_OK;
+}
+
+edxr_status edxr_resize(edxr_renderer* r, uint32_t width, uint32_t height)
+{
+    if (!r)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL renderer");
+    if (width == 0 || height == 0 || width > 32768 || height > 32768)
+        return fail(EDXR_ERR_INVALID_ARG, "framebuffer size must be in [1, 32768]");
+    DeviceGuard g(r->device);
+    edxr_status s = sync_pass(r);
+    if (s != EDXR_OK)
+        return s;
+    r->width = width;
+    r->height = height;
+    return EDXR_OK;
+}
+
+edxr_status edxr_set_transform(edxr_renderer* r, const float mv[16], const float proj[16], const float raster[16])
+{
+    if (!r || !mv || !proj || !raster)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    std::memcpy(r->cam.mv, mv, 64);
+    std::memcpy(r->cam.proj, proj, 64);
+    std::memcpy(r->cam.raster, raster, 64);
+    r->cam.set = true;
+    return EDXR_OK;
+}
+
+edxr_status edxr_set_state(edxr_renderer* r, const edxr_state* s)
+{
+    if (!r || !s)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    if (s->depth_func != EDXR_DEPTH_LEQUAL && s->depth_func != EDXR_DEPTH_LESS)
+        return fail(EDXR_ERR_INVALID_ARG, "unknown depth function");
+    if (s->msaa_log2 != 0)
+        return fail(EDXR_ERR_UNSUPPORTED, "multisampling is not provided by this build (msaa_log2 must be 0)");
+    r->state = *s;
+    return EDXR_OK;
+}
+
+edxr_status edxr_set_shader(edxr_renderer* r, int vs_kind, int ps_kind, const edxr_shader_params* p)
+{
+    if (!r)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL renderer");
+    if (vs_kind != EDXR_VS_DEFAULT)
+        return fail(EDXR_ERR_INVALID_ARG, "unknown vertex shader");
+    if (ps_kind < EDXR_PS_BLINN_PHONG || ps_kind > EDXR_PS_LAMBERTIAN)
+        return fail(EDXR_ERR_INVALID_ARG, "unknown pixel shader");
+    r->shading.ps_kind = ps_kind;
+    if (p)
+    {
+        const double n = std::sqrt((double)p->light[0] * p->light[0] + (double)p->light[1] * p->light[1] +
+                                   (double)p->light[2] * p->light[2]);
+        if (!(n > 0.0) || !std::isfinite(n))
+            return fail(EDXR_ERR_INVALID_ARG, "light direction must be a finite non-zero vector");
+        r->shading.p = *p;
+    }
+    return EDXR_OK;
+}
+
+edxr_status edxr_render(edxr_renderer* r, const edxr_mesh* mesh)
+{
+    if (!r)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL renderer");
+    if (!r->cam.set)
+        return fail(EDXR_ERR_INVALID_ARG, "edxr_set_transform was not called");
+    edxr_status s = check_mesh(mesh);
+    if (s != EDXR_OK)
+        return s;
+    DeviceGuard g(r->device);
+    if ((s = sync_pass(r)) != EDXR_OK)
+        return s;
+    edxr_mesh dm;
+    if ((s = stage_mesh(r, 0, mesh, &dm)) != EDXR_OK)
+        return s;
+    if ((s = ensure_frames_host(r, 1)) != EDXR_OK)
+        return s;
+    cudaEventSynchronize(r->done);  // the pinned descriptor may still be in flight
+    fill_frame(r->frames_host[0], dm, r->cam, r->shading, r->state.depth_func, r->state.hierarchical, r->width,
+               r->height);
+    return launch_frames(r, 1, r->width, r->height);
+}
+
+edxr_status edxr_synchronize(edxr_renderer* r)
+{
+    if (!r)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL renderer");
+    DeviceGuard g(r->device);
+    return sync_pass(r);
+}
+
+edxr_status edxr_get_outputs(edxr_renderer* r, edxr_outputs* out)
+{
+    if (!r || !out)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    DeviceGuard g(r->device);
+    edxr_status s = sync_pass(r);
+    if (s != EDXR_OK)
+        return s;
+    if (!r->last_frames)
+        return fail(EDXR_ERR_INVALID_ARG, "nothing rendered yet");
+    out->color = r->color.as<float>();
+    out->depth = r->depth.as<float>();
+    out->triangle_id = r->tri_id.as<uint32_t>();
+    out->width = r->out_width;
+    out->height = r->out_height;
+    return EDXR_OK;
+}
+
+edxr_status edxr_read_outputs(edxr_renderer* r, float* color, float* depth, uint32_t* id)
+{
+    if (!r)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL renderer");
+    DeviceGuard g(r->device);
+    edxr_status s = sync_pass(r);
+    if (s != EDXR_OK)
+        return s;
+    if (!r->last_frames)
+        return fail(EDXR_ERR_INVALID_ARG, "nothing rendered yet");
+    const size_t n = (size_t)r->out_width * r->out_height;
+    if (color) EDXR_CUDA(cudaMemcpyAsync(color, r->color.ptr, 16 * n, cudaMemcpyDeviceToHost, r->stream));
+    if (depth) EDXR_CUDA(cudaMemcpyAsync(depth, r->depth.ptr, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    if (id) EDXR_CUDA(cudaMemcpyAsync(id, r->tri_id.ptr, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    EDXR_CUDA(cudaStreamSynchronize(r->stream));
+    return EDXR_OK;
+}
+
+edxr_status edxr_get_back_buffer(edxr_renderer* r, const uint8_t** rgba8)
+{
+    if (!r || !rgba8)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    DeviceGuard g(r->device);
+    edxr_status s = sync_pass(r);
+    if (s != EDXR_OK)
+        return s;
+    if (!r->last_frames)
+        return fail(EDXR_ERR_INVALID_ARG, "nothing rendered yet");
+    const size_t n = (size_t)r->out_width * r->out_height;
+    EDXR_CUDA(r->back8.ensure(4 * n));
+    EDXR_CUDA(launch_back_buffer(r->color.as<float4>(), r->back8.as<uint8_t>(), (int)r->out_width,
+                                 (int)r->out_height, r->stream));
+    r->back_host.resize(4 * n);
+    EDXR_CUDA(cudaMemcpyAsync(r->back_host.data(), r->back8.ptr, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    EDXR_CUDA(cudaStreamSynchronize(r->stream));
+    *rgba8 = r->back_host.data();
+    return EDXR_OK;
+}
+
+edxr_status edxr_get_stats(edxr_renderer* r, edxr_stats* st)
+{
+    if (!r || !st)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    DeviceGuard g(r->device);
+    edxr_status s = sync_pass(r);
+    if (s != EDXR_OK)
+        return s;
+    st->raster_triangles = r->status_host->raster_tris;
+    st->bin_entries = r->status_host->bins_needed;
+    st->bin_capacity = r->bin_capacity;
+    st->rerenders = r->rerenders;
+    st->tile_size = kTileSize;
+    st->kernels_per_pass = r->last_frames ? (uint32_t)kernels_per_pass(r->last) : 0u;
+    st->clipped_polygons = r->status_host->clipped_polys;
+    return EDXR_OK;
+}
+
+edxr_status edxr_set_profiling(edxr_renderer* r, int enable)
+{
+    if (!r)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL renderer");
+    DeviceGuard g(r->device);
+    edxr_status s = sync_pass(r);
+    if (s != EDXR_OK)
+        return s;
+    if (enable && !r->stage_ev[0])
+        for (int i = 0; i < kStageEvents; i++)
+            EDXR_CUDA(cudaEventCreate(&r->stage_ev[i]));
+    r->profiling = enable != 0;
+    return EDXR_OK;
+}
+
+edxr_status edxr_get_stage_times(edxr_renderer* r, float* ms, uint32_t* count)
+{
+    if (!r || !ms || !count)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    if (!r->profiling)
+        return fail(EDXR_ERR_INVALID_ARG, "profiling is not enabled");
+    DeviceGuard g(r->device);
+    edxr_status s = sync_pass(r);
+    if (s != EDXR_OK)
+        return s;
+    const uint32_t n = std::min<uint32_t>(*count, kStageEvents - 1);
+    for (uint32_t i = 0; i < n; i++)
+        EDXR_CUDA(cudaEventElapsedTime(&ms[i], r->stage_ev[i], r->stage_ev[i + 1]));
+    *count = n;
+    return EDXR_OK;
+}
+
+edxr_status edxr_render_batched(edxr_renderer* r, const edxr_mesh* meshes, uint32_t num_meshes,
+                                const edxr_view* views, uint32_t num_views, uint32_t width, uint32_t height)
+{
+    if (!r || !meshes || !views || num_meshes == 0 || num_views == 0)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL or empty argument");
+    if (width == 0 || height == 0 || width > 32768 || height > 32768)
+        return fail(EDXR_ERR_INVALID_ARG, "framebuffer size must be in [1, 32768]");
+    edxr_status s;
+    for (uint32_t m = 0; m < num_meshes; m++)
+        if ((s = check_mesh(&meshes[m])) != EDXR_OK)
+            return s;
+    for (uint32_t v = 0; v < num_views; v++)
+    {
+        if (views[v].mesh >= num_meshes)
+            return fail(EDXR_ERR_INVALID_ARG, "view references a mesh out of range");
+        if (views[v].ps_kind < EDXR_PS_BLINN_PHONG || views[v].ps_kind > EDXR_PS_LAMBERTIAN)
+            return fail(EDXR_ERR_INVALID_ARG, "unknown pixel shader in view");
+        if (views[v].depth_func != EDXR_DEPTH_LEQUAL && views[v].depth_func != EDXR_DEPTH_LESS)
+            return fail(EDXR_ERR_INVALID_ARG, "unknown depth function in view");
+    }
+    DeviceGuard g(r->device);
+    if ((s = sync_pass(r)) != EDXR_OK)
+        return s;
+    std::vector<edxr_mesh> dm(num_meshes);
+    for (uint32_t m = 0; m < num_meshes; m++)
+        if ((s = stage_mesh(r, m, &meshes[m], &dm[m])) != EDXR_OK)
+            return s;
+    if ((s = ensure_frames_host(r, num_views)) != EDXR_OK)
+        return s;
+    cudaEventSynchronize(r->done);
+    for (uint32_t v = 0; v < num_views; v++)
+    {
+        Camera cam;
+        std::memcpy(cam.mv, views[v].mv, 64);
+        std::memcpy(cam.proj, views[v].proj, 64);
+        std::memcpy(cam.raster, views[v].raster, 64);
+        cam.set = true;
+        Shading sh;
+        sh.ps_kind = views[v].ps_kind;
+        sh.p = views[v].shading;
+        fill_frame(r->frames_host[v], dm[views[v].mesh], cam, sh, views[v].depth_func, r->state.hierarchical, width,
+                   height);
+    }
+    return launch_frames(r, num_views, width, height);
+}
+
+edxr_status edxr_get_batch_outputs(edxr_renderer* r, edxr_batch_outputs* out)
+{
+    if (!r || !out)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    DeviceGuard g(r->device);
+    edxr_status s = sync_pass(r);
+    if (s != EDXR_OK)
+        return s;
+    if (!r->last_frames)
+        return fail(EDXR_ERR_INVALID_ARG, "nothing rendered yet");
+    out->color = r->color.as<float>();
+    out->depth = r->depth.as<float>();
+    out->triangle_id = r->tri_id.as<uint32_t>();
+    out->num_views = r->last_frames;
+    out->width = r->out_width;
+    out->height = r->out_height;
+    return EDXR_OK;
+}
+
+edxr_status edxr_shade_visible(edxr_renderer* r, const edxr_mesh* mesh, float* color_out)
+{
+    (void)mesh; (void)color_out;
+    if (!r)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL renderer");
+    return fail(EDXR_ERR_UNSUPPORTED, "edxr_shade_visible is not built yet");
+}
+
+edxr_status edxr_backward(edxr_renderer* r, const edxr_mesh* mesh, const float* grad_color, const edxr_grads* grads)
+{
+    (void)mesh; (void)grad_color; (void)grads;
+    if (!r)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL renderer");
+    return fail(EDXR_ERR_UNSUPPORTED, "edxr_backward is not built yet");
+}
+
+}  // extern "C"

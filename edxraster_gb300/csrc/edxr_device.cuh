@@ -1,0 +1,542 @@
+// Device-side arithmetic of the EDXRaster pipeline.
+//
+// Integer work is int32 with wraparound (the reference's SSE paddd / pmulld);
+// it is written through uint32_t so no signed overflow is relied upon.  Every
+// float operation that feeds coverage, depth or the winning triangle uses the
+// explicit round-to-nearest intrinsics (__fmul_rn, __fadd_rn, __fdiv_rn ...)
+// so the compiler can never contract or reorder it; the library is also
+// built with -fmad=false.
+#pragma once
+
+#include "edxr_internal.h"
+
+namespace edxr {
+
+__device__ __forceinline__ int wadd(int a, int b) { return (int)((uint32_t)a + (uint32_t)b); }
+__device__ __forceinline__ int wsub(int a, int b) { return (int)((uint32_t)a - (uint32_t)b); }
+__device__ __forceinline__ int wmul(int a, int b) { return (int)((uint32_t)a * (uint32_t)b); }
+
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+
+// Matrix::TransformPoint(Vector4(p, 1)) (Shader.h:45): row i is summed left to
+// right, ((m0*x + m1*y) + m2*z) + m3*1.
+__device__ __forceinline__ float4 xform_point4(const float* M, float x, float y, float z)
+{
+    float o[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+    {
+        float s = fmul(M[i * 4 + 0], x);
+        s = fadd(s, fmul(M[i * 4 + 1], y));
+        s = fadd(s, fmul(M[i * 4 + 2], z));
+        s = fadd(s, fmul(M[i * 4 + 3], 1.0f));
+        o[i] = s;
+    }
+    return make_float4(o[0], o[1], o[2], o[3]);
+}
+
+// Matrix::TransformPoint(Vector3) with the raster matrix (RasterTriangle.h:30-32):
+// homogeneous divide only when the resulting w is not exactly one.
+__device__ __forceinline__ void xform_point3(const float* M, float x, float y, float z, float& ox, float& oy)
+{
+    float o[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+    {
+        float s = fmul(M[i * 4 + 0], x);
+        s = fadd(s, fmul(M[i * 4 + 1], y));
+        s = fadd(s, fmul(M[i * 4 + 2], z));
+        s = fadd(s, M[i * 4 + 3]);
+        o[i] = s;
+    }
+    if (o[3] == 1.0f)
+    {
+        ox = o[0];
+        oy = o[1];
+    }
+    else
+    {
+        ox = fdiv(o[0], o[3]);
+        oy = fdiv(o[1], o[3]);
+    }
+}
+
+// v.x = a.x * 16.0 (RasterTriangle.h:35-40): the product is taken in double and
+// truncated toward zero; NaN and out-of-range give INT_MIN, as the x86
+// cvttsd2si conversion of the reference does.
+__device__ __forceinline__ int snap16(float f)
+{
+    const double d = __dmul_rn((double)f, 16.0);
+    if (!(d > -2147483649.0 && d < 2147483648.0))
+        return (int)0x80000000;
+    return __double2int_rz(d);
+}
+
+// Clipper::ComputeClipCode (Clipper.h:48-68).
+enum : uint32_t { kLeft = 1, kRight = 2, kBottom = 4, kTop = 8, kNear = 16, kFar = 32 };
+
+__device__ __forceinline__ uint32_t clip_code(float4 v)
+{
+    uint32_t c = 0;
+    if (v.x < -v.w) c |= kLeft;
+    if (v.x > v.w) c |= kRight;
+    if (v.y < -v.w) c |= kBottom;
+    if (v.y > v.w) c |= kTop;
+    if (v.z > v.w) c |= kFar;
+    if (v.z < 0.0f) c |= kNear;
+    return c;
+}
+
+__device__ __forceinline__ bool plane_inside(int plane, float4 v)
+{
+    switch (plane)
+    {
+    case 0: return v.x >= -v.w;
+    case 1: return v.x <= v.w;
+    case 2: return v.y >= -v.w;
+    case 3: return v.y <= v.w;
+    case 4: return v.z <= v.w;
+    default: return v.z >= 0.0f;
+    }
+}
+
+// t of the intersection, exactly as written in Clipper.h:241-276.
+__device__ __forceinline__ float plane_t(int plane, float4 a, float4 b)
+{
+    switch (plane)
+    {
+    case 0: return fdiv(fadd(a.w, a.x), fsub(fadd(a.x, a.w), fadd(b.x, b.w)));
+    case 1: return fdiv(fadd(-a.w, a.x), fsub(fsub(a.x, a.w), fsub(b.x, b.w)));
+    case 2: return fdiv(fadd(a.w, a.y), fsub(fadd(a.y, a.w), fadd(b.y, b.w)));
+    case 3: return fdiv(fadd(-a.w, a.y), fsub(fsub(a.y, a.w), fsub(b.y, b.w)));
+    case 4: return fdiv(fadd(-a.w, a.z), fsub(fsub(a.z, a.w), fsub(b.z, b.w)));
+    default: return fdiv(a.z, fsub(a.z, b.z));
+    }
+}
+
+struct PolyVert
+{
+    float4 p;
+    float w0, w1, w2;
+};
+
+// Intersection vertex (Clipper.h:210-214,221-224): v0*(1-t) + v1*t, snapped
+// onto the plane, and the clip weights blended with the same factors.
+__device__ __forceinline__ PolyVert plane_cut(int plane, const PolyVert& a, const PolyVert& b)
+{
+    const float t = plane_t(plane, a.p, b.p);
+    const float s = fsub(1.0f, t);
+    PolyVert r;
+    r.p.x = fadd(fmul(a.p.x, s), fmul(b.p.x, t));
+    r.p.y = fadd(fmul(a.p.y, s), fmul(b.p.y, t));
+    r.p.z = fadd(fmul(a.p.z, s), fmul(b.p.z, t));
+    r.p.w = fadd(fmul(a.p.w, s), fmul(b.p.w, t));
+    switch (plane)
+    {
+    case 0: r.p.x = -r.p.w; break;
+    case 1: r.p.x = r.p.w; break;
+    case 2: r.p.y = -r.p.w; break;
+    case 3: r.p.y = r.p.w; break;
+    case 4: r.p.z = r.p.w; break;
+    default: r.p.z = 0.0f; break;
+    }
+    r.w0 = fadd(fmul(a.w0, s), fmul(b.w0, t));
+    r.w1 = fadd(fmul(a.w1, s), fmul(b.w1, t));
+    r.w2 = fadd(fmul(a.w2, s), fmul(b.w2, t));
+    return r;
+}
+
+// Clipper::ClipPolygon (Clipper.h:235-288): Sutherland-Hodgman against the
+// planes in planeCode, in the order L, R, B, T, F, N, then the polygon is
+// dropped when any vertex has w <= 0.  Returns the vertex count.
+__device__ __noinline__ int clip_polygon(PolyVert* poly, uint32_t planeCode)
+{
+    PolyVert tmp[kMaxPolygon];
+    int n = 3;
+    const uint32_t bits[6] = { kLeft, kRight, kBottom, kTop, kFar, kNear };
+    for (int k = 0; k < 6; k++)
+    {
+        if (!(planeCode & bits[k]))
+            continue;
+        int m = 0;
+        for (int i = 0; i < n; i++)
+        {
+            const int i1 = (i + 1 == n) ? 0 : i + 1;
+            const bool in0 = plane_inside(k, poly[i].p);
+            const bool in1 = plane_inside(k, poly[i1].p);
+            if (in0)
+            {
+                if (m < kMaxPolygon) tmp[m++] = in1 ? poly[i1] : plane_cut(k, poly[i], poly[i1]);
+            }
+            else if (in1)
+            {
+                if (m < kMaxPolygon) tmp[m++] = plane_cut(k, poly[i], poly[i1]);
+                if (m < kMaxPolygon) tmp[m++] = poly[i1];
+            }
+        }
+        for (int i = 0; i < m; i++)
+            poly[i] = tmp[i];
+        n = m;
+    }
+    for (int i = 0; i < n; i++)
+        if (poly[i].p.w <= 0.0f)
+            return 0;
+    return n;
+}
+
+// Reject / accept corner of one edge from the sign of B / float(C) and of C
+// (RasterTriangle.h:66-150); packed as rej | acc << 2.
+__device__ __forceinline__ uint32_t corner_code(int B, int C)
+{
+    const float slope = fdiv(__int2float_rn(B), __int2float_rn(C));
+    const bool cpos = __int2float_rn(C) >= 0.0f;
+    uint32_t rej, acc;
+    if (slope >= 0.0f) { rej = cpos ? 3u : 0u; acc = cpos ? 0u : 3u; }
+    else { rej = cpos ? 2u : 1u; acc = cpos ? 1u : 2u; }
+    return rej | (acc << 2);
+}
+
+// RasterTriangle::Setup (RasterTriangle.h:27-153) for three clip-space
+// vertices, plus the post-pass of Renderer.cpp:139-147 (invW = 1/w,
+// z *= invW).  Returns false for back-facing or degenerate triangles.
+__device__ __forceinline__ bool setup_triangle(const FrameDesc& f, float4 c0, float4 c1, float4 c2, RTri& t)
+{
+    const float4 cs[3] = { c0, c1, c2 };
+    int vx[3], vy[3];
+    float zp[3], iw[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        const float invW = fdiv(1.0f, cs[k].w);
+        const float hx = fmul(cs[k].x, invW), hy = fmul(cs[k].y, invW), hz = fmul(cs[k].z, invW);
+        float rx, ry;
+        xform_point3(f.raster, hx, hy, hz, rx, ry);
+        vx[k] = snap16(rx);
+        vy[k] = snap16(ry);
+        zp[k] = hz;
+        iw[k] = invW;
+    }
+    const int B0 = wsub(vy[0], vy[1]), C0 = wsub(vx[1], vx[0]);
+    const int B1 = wsub(vy[1], vy[2]), C1 = wsub(vx[2], vx[1]);
+    const int B2 = wsub(vy[2], vy[0]), C2 = wsub(vx[0], vx[2]);
+    const int det = wsub(wmul(C2, B1), wmul(C1, B2));
+    if (det <= 0)
+        return false;
+    t.v0x = vx[0]; t.v0y = vy[0];
+    t.v1x = vx[1]; t.v1y = vy[1];
+    t.v2x = vx[2]; t.v2y = vy[2];
+    t.invDet = fdiv(1.0f, __int2float_rn(det));
+    t.z0 = zp[0]; t.z1 = zp[1]; t.z2 = zp[2];
+    t.invW0 = iw[0]; t.invW1 = iw[1]; t.invW2 = iw[2];
+    t.meta = corner_code(B0, C0) | (corner_code(B1, C1) << 4) | (corner_code(B2, C2) << 8);
+    return true;
+}
+
+// Edge coefficients B, C of a setup triangle (RasterTriangle.h:42-47).
+struct Edges
+{
+    int B[3], C[3];
+    int vx[3], vy[3];
+};
+
+__device__ __forceinline__ Edges tri_edges(const RTri& t)
+{
+    Edges e;
+    e.vx[0] = t.v0x; e.vy[0] = t.v0y;
+    e.vx[1] = t.v1x; e.vy[1] = t.v1y;
+    e.vx[2] = t.v2x; e.vy[2] = t.v2y;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        const int n = (k + 1) % 3;
+        e.B[k] = wsub(e.vy[k], e.vy[n]);
+        e.C[k] = wsub(e.vx[n], e.vx[k]);
+    }
+    return e;
+}
+
+// Top-left bias of the scalar edge functions used by binning and the coarse
+// step (RasterTriangle.h:155-158): 0 on a top-left edge, else -1.
+__device__ __forceinline__ int tl_scalar(int ax, int ay, int bx, int by)
+{
+    return ((by > ay) || (ay == by && ax > bx)) ? 0 : -1;
+}
+// Bias of the 4-wide pixel edge functions (RasterTriangle.h:296-299): the
+// comparison mask converts to -1 on a top-left edge, else 0.
+__device__ __forceinline__ int tl_pixel(int ax, int ay, int bx, int by)
+{
+    return ((by > ay) || (ay == by && ax > bx)) ? -1 : 0;
+}
+
+// EdgeFunc0..2 (RasterTriangle.h:160-171).
+__device__ __forceinline__ int edge_scalar(const Edges& e, int k, int px, int py)
+{
+    const int n = (k + 1) % 3;
+    return wadd(wadd(wmul(e.B[k], wsub(px, e.vx[k])), wmul(e.C[k], wsub(py, e.vy[k]))),
+                tl_scalar(e.vx[k], e.vy[k], e.vx[n], e.vy[n]));
+}
+
+// Lane q of GenStepVectors (RasterTriangle.h:192-255) for one edge.
+__device__ __forceinline__ int step_lane(uint32_t corner, int B, int C, int q)
+{
+    int v;
+    switch (corner)
+    {
+    case 0: v = (q == 0) ? 0 : (q == 1) ? B : (q == 2) ? C : wadd(B, C); break;
+    case 1: v = (q == 0) ? wsub(0, B) : (q == 1) ? 0 : (q == 2) ? wsub(C, B) : C; break;
+    case 2: v = (q == 0) ? wsub(0, C) : (q == 1) ? wsub(B, C) : (q == 2) ? 0 : B; break;
+    default: v = (q == 0) ? wsub(wsub(0, B), C) : (q == 1) ? wsub(0, C) : (q == 2) ? wsub(0, B) : 0; break;
+    }
+    return wmul(256, v);  // stepSize = blockSize << 3 with blockSize = 32
+}
+
+// Per-triangle binning geometry.
+struct BinGeom
+{
+    int bbx0, bbx1, bby0, bby1;      // pixel bounding box (v >> 4)
+    int t32x0, t32x1, t32y0, t32y1;  // reference 32x32 tile range (Renderer.cpp:168-171)
+    int t16x0, t16x1, t16y0, t16y1;  // candidate 16x16 tiles
+    bool small;                      // Renderer.cpp:173
+};
+
+__device__ __forceinline__ BinGeom bin_geom(const RTri& t, const FrameDesc& f)
+{
+    BinGeom g;
+    const int minx = min(t.v0x, min(t.v1x, t.v2x)), maxx = max(t.v0x, max(t.v1x, t.v2x));
+    const int miny = min(t.v0y, min(t.v1y, t.v2y)), maxy = max(t.v0y, max(t.v1y, t.v2y));
+    g.bbx0 = minx >> 4; g.bbx1 = maxx >> 4;
+    g.bby0 = miny >> 4; g.bby1 = maxy >> 4;
+    g.t32x0 = max(0, minx >> 9); g.t32x1 = min(f.tdx32 - 1, maxx >> 9);
+    g.t32y0 = max(0, miny >> 9); g.t32y1 = min(f.tdy32 - 1, maxy >> 9);
+    g.small = (g.t32x1 - g.t32x0 < 2) && (g.t32y1 - g.t32y0 < 2);
+    g.t16x0 = g.t32x0 * 2; g.t16x1 = min(f.tdx - 1, g.t32x1 * 2 + 1);
+    g.t16y0 = g.t32y0 * 2; g.t16y1 = min(f.tdy - 1, g.t32y1 * 2 + 1);
+    return g;
+}
+
+// Does the fine-raster region of the reference (the quad-aligned bounding
+// box, Rasterizer.h:132-140) touch an on-screen pixel of 16x16 tile (tx, ty)?
+__device__ __forceinline__ bool fine_region_hits(const BinGeom& g, const FrameDesc& f, int tx, int ty)
+{
+    const int x0 = max(tx * kTileSize, g.bbx0 & ~1);
+    const int x1 = min(min(tx * kTileSize + kTileSize - 1, f.width - 1), g.bbx1 | 1);
+    const int y0 = max(ty * kTileSize, g.bby0 & ~1);
+    const int y1 = min(min(ty * kTileSize + kTileSize - 1, f.height - 1), g.bby1 | 1);
+    return x0 <= x1 && y0 <= y1;
+}
+
+// The reference's treatment of 16x16 tile (tx, ty) for triangle t: 0 (not
+// rasterized), kDecisionAccept (TrivialAcceptTriangle: every pixel is
+// depth-tested) or kDecisionFine (FineRasterize: edge test per pixel inside
+// the quad-aligned bounding box).  Follows the binning of
+// Renderer.cpp:173-227, RasterizeTile (Renderer.cpp:248-270) and
+// CoarseRasterize (Rasterizer.h:32-111) with their int32 wraparound.
+__device__ __forceinline__ uint32_t tile_decision(const RTri& t, const Edges& e, const BinGeom& g,
+                                                  const FrameDesc& f, int tx, int ty)
+{
+    const int T32x = tx >> 1, T32y = ty >> 1;
+    if (T32x < g.t32x0 || T32x > g.t32x1 || T32y < g.t32y0 || T32y > g.t32y1)
+        return 0;
+    if (g.small)
+        return fine_region_hits(g, f, tx, ty) ? kDecisionFine : 0;
+
+    const int shift = kRefTileLog2 + 4;
+    uint32_t rej[3], acc[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        rej[k] = (t.meta >> (4 * k)) & 3u;
+        acc[k] = (t.meta >> (4 * k + 2)) & 3u;
+    }
+    bool accE[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        const int cx = (T32x + (int)(rej[k] & 1)) << shift;
+        const int cy = (T32y + (int)(rej[k] >> 1)) << shift;
+        if (edge_scalar(e, k, cx, cy) < 0)
+            return 0;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        const int cx = (T32x + (int)(acc[k] & 1)) << shift;
+        const int cy = (T32y + (int)(acc[k] >> 1)) << shift;
+        accE[k] = edge_scalar(e, k, cx, cy) >= 0;
+    }
+    if (accE[0] && accE[1] && accE[2])
+        return kDecisionAccept;
+    if (!f.hierarchical)
+        return fine_region_hits(g, f, tx, ty) ? kDecisionFine : 0;
+
+    // CoarseRasterize on the 32x32 tile, quadrant q of this 16x16 tile.
+    const int q = (tx & 1) + 2 * (ty & 1);
+    const int baseX = (T32x << kRefTileLog2) << 4, baseY = (T32y << kRefTileLog2) << 4;
+    const int span = (32 << 4) - 1;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        const int re = edge_scalar(e, k, baseX + (int)(rej[k] & 1) * span, baseY + (int)(rej[k] >> 1) * span);
+        if (wadd(re, step_lane(rej[k], e.B[k], e.C[k], q)) < 0)
+            return 0;
+    }
+    bool all = true;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        if (accE[k])
+            continue;  // IntSSE(EDX_INFINITY): this edge always accepts
+        const int ae = edge_scalar(e, k, baseX + (int)(acc[k] & 1) * span, baseY + (int)(acc[k] >> 1) * span);
+        all = all && (wadd(ae, step_lane(acc[k], e.B[k], e.C[k], q)) >= 0);
+    }
+    if (all)
+        return kDecisionAccept;
+    return fine_region_hits(g, f, tx, ty) ? kDecisionFine : 0;
+}
+
+// Monotone key of a depth value: -0 and +0 share a key, float order is
+// preserved for all non-NaN values.
+__device__ __forceinline__ uint32_t depth_key(float d)
+{
+    const uint32_t u = __float_as_uint(d == 0.0f ? 0.0f : d);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 normalize3(float3 v)
+{
+    const float inv = 1.0f / sqrtf(dot3(v, v));
+    return f3(v.x * inv, v.y * inv, v.z * inv);
+}
+__device__ __forceinline__ float3 ld3(const char* base, uint32_t stride, uint32_t i, float dflt)
+{
+    if (!base)
+        return f3(dflt, dflt, dflt);
+    const float* p = reinterpret_cast<const float*>(base + (size_t)i * stride);
+    return f3(__ldg(p), __ldg(p + 1), __ldg(p + 2));
+}
+
+// Per-pixel shading inputs of a triangle: its three vertices' position,
+// normal and albedo (after clipping) in object space.
+struct ShadeVerts
+{
+    float3 p[3], n[3], a[3];
+};
+
+// Attributes of the raster vertices of triangle t (Clipper.h:138-151 for the
+// vertices the clipper created: weight.x*a0 + weight.y*a1 + weight.z*a2).
+__device__ __forceinline__ ShadeVerts shade_verts(const FrameDesc& f, const RTri& t, const ClipPoly* polys)
+{
+    const uint32_t tri = t.order >> 4;
+    const uint32_t i0 = __ldg(f.indices + 3 * (size_t)tri + 0);
+    const uint32_t i1 = __ldg(f.indices + 3 * (size_t)tri + 1);
+    const uint32_t i2 = __ldg(f.indices + 3 * (size_t)tri + 2);
+    float3 sp[3] = { ld3(f.positions, f.pos_stride, i0, 0.f), ld3(f.positions, f.pos_stride, i1, 0.f), ld3(f.positions, f.pos_stride, i2, 0.f) };
+    float3 sn[3] = { ld3(f.normals, f.nrm_stride, i0, 0.f), ld3(f.normals, f.nrm_stride, i1, 0.f), ld3(f.normals, f.nrm_stride, i2, 0.f) };
+    float3 sa[3] = { ld3(f.albedo, f.alb_stride, i0, 1.f), ld3(f.albedo, f.alb_stride, i1, 1.f), ld3(f.albedo, f.alb_stride, i2, 1.f) };
+    ShadeVerts v;
+    if (t.poly == kUnclipped)
+    {
+#pragma unroll
+        for (int k = 0; k < 3; k++) { v.p[k] = sp[k]; v.n[k] = sn[k]; v.a[k] = sa[k]; }
+        return v;
+    }
+    const ClipPoly& P = polys[t.poly >> 4];
+    const int fk = (int)(t.poly & 15u);
+    const int pv[3] = { 0, fk - 1, fk };
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        const float w0 = P.w[pv[k]][0], w1 = P.w[pv[k]][1], w2 = P.w[pv[k]][2];
+        v.p[k] = f3(fadd(fadd(fmul(w0, sp[0].x), fmul(w1, sp[1].x)), fmul(w2, sp[2].x)),
+                    fadd(fadd(fmul(w0, sp[0].y), fmul(w1, sp[1].y)), fmul(w2, sp[2].y)),
+                    fadd(fadd(fmul(w0, sp[0].z), fmul(w1, sp[1].z)), fmul(w2, sp[2].z)));
+        v.n[k] = f3(fadd(fadd(fmul(w0, sn[0].x), fmul(w1, sn[1].x)), fmul(w2, sn[2].x)),
+                    fadd(fadd(fmul(w0, sn[0].y), fmul(w1, sn[1].y)), fmul(w2, sn[2].y)),
+                    fadd(fadd(fmul(w0, sn[0].z), fmul(w1, sn[1].z)), fmul(w2, sn[2].z)));
+        v.a[k] = f3(fadd(fadd(fmul(w0, sa[0].x), fmul(w1, sa[1].x)), fmul(w2, sa[2].x)),
+                    fadd(fadd(fmul(w0, sa[0].y), fmul(w1, sa[1].y)), fmul(w2, sa[2].y)),
+                    fadd(fadd(fmul(w0, sa[0].z), fmul(w1, sa[1].z)), fmul(w2, sa[2].z)));
+    }
+    return v;
+}
+
+// The shading model on interpolated attributes (Shader.h:249-281 structure):
+//   N = normalize(n), L = light, E = normalize(eye - p), H = normalize(L + E)
+//   diffuse = (max(N.L, 0) + 0.2) * 3/pi
+//   BLINN_PHONG:           albedo*diffuse + ks*max(N.H, 0)^shininess
+//   BLINN_PHONG_REFERENCE: diffuse + ks*(N.H)^shininess
+//   LAMBERTIAN_ALBEDO:     albedo*diffuse
+//   LAMBERTIAN:            diffuse
+__device__ __forceinline__ float3 shade_model(const FrameDesc& f, float3 P, float3 Nraw, float3 A)
+{
+    const float3 N = normalize3(Nraw);
+    const float3 L = f3(f.light[0], f.light[1], f.light[2]);
+    const float nl = fmaxf(dot3(L, N), 0.0f);
+    const float diffuse = (nl + 0.2f) * 0.954929658551372f;  // 3/pi
+    float spec = 0.0f;
+    if (f.ps_kind <= 1)
+    {
+        const float3 E = normalize3(f3(f.eye[0] - P.x, f.eye[1] - P.y, f.eye[2] - P.z));
+        const float3 H = normalize3(f3(L.x + E.x, L.y + E.y, L.z + E.z));
+        float nh = dot3(N, H);
+        if (f.ps_kind == 0)
+            nh = fmaxf(nh, 0.0f);
+        spec = f.ks * powf(nh, f.shininess);
+    }
+    switch (f.ps_kind)
+    {
+    case 0: return f3(A.x * diffuse + spec, A.y * diffuse + spec, A.z * diffuse + spec);
+    case 1: return f3(diffuse + spec, diffuse + spec, diffuse + spec);
+    case 2: return f3(A.x * diffuse, A.y * diffuse, A.z * diffuse);
+    default: return f3(diffuse, diffuse, diffuse);
+    }
+}
+
+// Fragment::Interpolate (Shader.h:142-170) from the fragment's barycentrics,
+// then the shading model.
+__device__ __forceinline__ float3 shade_fragment(const FrameDesc& f, const RTri& t, const ClipPoly* polys,
+                                                 float l0, float l1)
+{
+    float b0 = l0, b1 = l1;
+    float b2 = fsub(fsub(1.0f, b0), b1);
+    b0 = fmul(b0, t.invW0);
+    b1 = fmul(b1, t.invW1);
+    b2 = fmul(b2, t.invW2);
+    const float invB = fdiv(1.0f, fadd(fadd(b0, b1), b2));
+    b0 = fmul(b0, invB);
+    b1 = fmul(b1, invB);
+    b2 = fsub(fsub(1.0f, b0), b1);
+    const ShadeVerts v = shade_verts(f, t, polys);
+    const float3 P = f3(b0 * v.p[0].x + b1 * v.p[1].x + b2 * v.p[2].x,
+                        b0 * v.p[0].y + b1 * v.p[1].y + b2 * v.p[2].y,
+                        b0 * v.p[0].z + b1 * v.p[1].z + b2 * v.p[2].z);
+    const float3 N = f3(b0 * v.n[0].x + b1 * v.n[1].x + b2 * v.n[2].x,
+                        b0 * v.n[0].y + b1 * v.n[1].y + b2 * v.n[2].y,
+                        b0 * v.n[0].z + b1 * v.n[1].z + b2 * v.n[2].z);
+    const float3 A = f3(b0 * v.a[0].x + b1 * v.a[1].x + b2 * v.a[2].x,
+                        b0 * v.a[0].y + b1 * v.a[1].y + b2 * v.a[2].y,
+                        b0 * v.a[0].z + b1 * v.a[1].z + b2 * v.a[2].z);
+    return shade_model(f, P, N, A);
+}
+
+// Frame owning flattened index i, by binary search over a monotone base
+// field (tri_base or tile_base) of the frame array.
+template <typename Get>
+__device__ __forceinline__ uint32_t find_frame(const FrameDesc* frames, uint32_t n, uint32_t i, Get get)
+{
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi)
+    {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (get(frames[mid]) <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+}  // namespace edxr

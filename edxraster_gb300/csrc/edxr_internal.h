@@ -1,0 +1,128 @@
+// Internal definitions shared by the host code and the CUDA kernels of the
+// EDXRaster GB300 pipeline.  Everything here is a layout in device memory.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace edxr {
+
+// 16x16-pixel bin tiles.  Each is exactly one quadrant of a 32x32 tile of the
+// reference (Tile::SIZE_LOG_2 = 5, Tile.h:12), so the reference's per-32-tile
+// and per-quadrant decisions (Renderer.cpp:173-227, Rasterizer.h:32-111) map
+// onto a 16x16 tile without change.
+constexpr int kTileLog2 = 4;
+constexpr int kTileSize = 1 << kTileLog2;
+constexpr int kRefTileLog2 = 5;
+
+// Decision of the reference for one (triangle, 16x16 tile) pair.
+constexpr uint32_t kDecisionAccept = 1;  // every pixel is depth-tested, no edge test
+constexpr uint32_t kDecisionFine = 2;    // pixel edge test inside the bounding box
+
+constexpr uint32_t kUnclipped = 0xFFFFFFFFu;
+constexpr uint32_t kNoTriangle = 0xFFFFFFFFu;
+// 3 + one vertex per clip plane is 9 in exact arithmetic; rounding on nearly
+// collinear vertices can add a few more, so the working polygon has room.
+constexpr int kMaxPolygon = 16;
+
+// Per frame (one view of one mesh).  Kernels read it from global memory.
+struct FrameDesc
+{
+    // mesh (device pointers; strides in bytes)
+    const char* positions; const char* normals; const char* albedo; const char* uvs;
+    const uint32_t* indices;
+    uint32_t pos_stride, nrm_stride, alb_stride, uv_stride;
+    uint32_t nv, nt;
+    // flattened work offsets of this frame
+    uint32_t vtx_base;   // into the clip-position buffer
+    uint32_t tri_base;   // into the flattened input-triangle space
+    uint32_t tile_base;  // into the flattened 16x16-tile space
+    uint32_t pad0;
+    uint64_t pix_base;   // into the output images
+    int width, height;
+    int tdx, tdy;        // 16x16 tile grid
+    int tdx32, tdy32;    // reference 32x32 tile grid
+    int ps_kind, depth_func, hierarchical, pad1;
+    float mvp[16];
+    float raster[16];
+    float eye[3];        // object-space eye position (MV^-1 * 0)
+    float light[3];      // normalised light direction
+    float ks, shininess;
+    float ndc_from_raster[6];  // 2D affine inverse of the raster matrix (x, y rows)
+};
+
+// One triangle after clipping and setup (RasterTriangle, RasterTriangle.h:11-24),
+// 64 bytes, written by the setup kernel in any order; `order` restores the
+// reference's submission order: input triangle * 16 + fan index.
+struct __align__(16) RTri
+{
+    int v0x, v0y, v1x, v1y;
+    int v2x, v2y;
+    uint32_t order;
+    uint32_t meta;       // bits 0-11: reject/accept corners (2 bits each), 12-31: frame index
+    float invDet, z0, z1, z2;   // z after the post-pass (z_clip * (1/w))
+    float invW0, invW1, invW2;
+    uint32_t poly;       // kUnclipped, or (clipped-polygon index << 4) | fan index
+};
+static_assert(sizeof(RTri) == 64, "RTri must stay 64 bytes");
+
+// Clip weights of the vertices of one clipped polygon (Clipper.h:123-152),
+// relative to the source triangle's three vertices.
+struct __align__(16) ClipPoly
+{
+    float w[kMaxPolygon][3];
+    uint32_t n;
+};
+
+// Device status word, read back after every frame.
+struct DeviceStatus
+{
+    uint32_t overflow;       // bins needed more than the capacity
+    uint32_t error;          // EDXR_ERR_TIMEOUT and similar
+    uint64_t bins_needed;    // padded bin entries this frame
+    uint32_t raster_tris;    // needed (may exceed the capacity)
+    uint32_t clipped_polys;  // needed
+    uint32_t big_tris;       // needed
+    uint32_t pad;
+};
+
+// Launch parameters shared by every kernel of one pass.
+struct PassArgs
+{
+    const FrameDesc* frames;
+    uint32_t num_frames;
+    uint32_t total_vertices;
+    uint32_t total_tris;
+    uint32_t total_tiles;
+    float4* clip;            // per (frame, vertex) clip position
+    RTri* rtris;
+    uint32_t rtri_capacity;
+    ClipPoly* polys;
+    uint32_t poly_capacity;
+    uint32_t* tile_count;    // total_tiles + 1
+    uint32_t* tile_offset;   // total_tiles + 1 (exclusive scan of padded counts)
+    uint32_t* tile_cursor;   // total_tiles
+    uint32_t* bins;
+    uint64_t bin_capacity;
+    uint32_t* big_list;      // raster triangles with many tiles, binned by whole blocks
+    uint32_t big_capacity;
+    uint32_t* counters;      // [0] raster tris, [1] polys, [2] big tris, [3] raster work queue
+    DeviceStatus* status;
+    float4* color;
+    float* depth;
+    uint32_t* tri_id;
+    int num_sms;
+};
+
+// Host-side launchers (edxr_kernels.cu).
+constexpr int kStageEvents = 7;  // boundaries of the 6 timed stages
+// ev: NULL, or kStageEvents events recorded around the stages.
+cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev = nullptr);
+int kernels_per_pass(const PassArgs& a);
+void prepare_kernels();
+cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s);
+cudaError_t launch_shade_visible(const PassArgs& a, float4* out, cudaStream_t s);
+cudaError_t launch_backward(const PassArgs& a, const float4* grad, float* g_alb, float* g_nrm, float* g_pos,
+                            float* g_light, float* g_ks, float* g_shin, cudaStream_t s);
+
+}  // namespace edxr

@@ -1,0 +1,639 @@
+// CUDA kernels of the EDXRaster GB300 pipeline (sm_103a).
+//
+// One pass renders any number of frames (a frame = one mesh seen by one
+// camera); the plain path is a pass of one frame.  Stages:
+//   k_clear        zero the per-tile counters and work queues
+//   k_vertex       clip = MVP * (p, 1) per (frame, vertex)     Shader.h:40-49
+//   k_setup        clip codes, clipping, fixed-point setup      Clipper.h:71-189,
+//                  and the post-pass, per input triangle        RasterTriangle.h:27-153
+//   k_bin*         (triangle, 16x16 tile) decisions, counted,   Renderer.cpp:161-229
+//                  scanned and scattered into per-tile bins
+//   k_raster       persistent tiles: coverage, depth, winner,   Renderer.cpp:248-350,
+//                  deferred shading of the winner, one write    Rasterizer.h:32-415
+//                  of colour, depth and triangle id per pixel   FrameBuffer.cpp:54-68
+#include <cuda_runtime.h>
+
+#include "edxr_device.cuh"
+
+namespace edxr {
+
+constexpr int kBigTiles = 64;          // candidate tiles above which a whole block bins a triangle
+constexpr int kRasterThreads = 256;    // one thread per pixel of a 16x16 tile
+constexpr int kScanItems = 4;
+constexpr int kScanThreads = 1024;
+constexpr int kScanBlock = kScanItems * kScanThreads;
+
+// -------------------------------------------------------------------------
+__global__ void k_clear(PassArgs a)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= a.total_tiles; i += stride)
+    {
+        a.tile_count[i] = 0;
+        a.tile_cursor[i] = 0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x < 8)
+        a.counters[threadIdx.x] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        a.status->overflow = 0;
+        a.status->error = 0;
+        a.status->bins_needed = 0;
+        a.status->raster_tris = 0;
+        a.status->clipped_polys = 0;
+        a.status->big_tris = 0;
+    }
+}
+
+// -------------------------------------------------------------------------
+// Vertex stage: one thread per (frame, vertex).
+__global__ void __launch_bounds__(256) k_vertex(PassArgs a)
+{
+    const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gi >= a.total_vertices)
+        return;
+    const uint32_t fi = find_frame(a.frames, a.num_frames, gi, [](const FrameDesc& f) { return f.vtx_base; });
+    const FrameDesc& f = a.frames[fi];
+    const uint32_t v = gi - f.vtx_base;
+    const float* p = reinterpret_cast<const float*>(f.positions + (size_t)v * f.pos_stride);
+    a.clip[gi] = xform_point4(f.mvp, __ldg(p), __ldg(p + 1), __ldg(p + 2));
+}
+
+// -------------------------------------------------------------------------
+// Clipping + setup: one thread per input triangle.  Surviving triangles are
+// appended with a warp-aggregated atomic; each carries its submission order.
+__device__ __forceinline__ void clip_triangle(const FrameDesc& f, float4 c0, float4 c1, float4 c2,
+                                              uint32_t planes, PolyVert* poly, int& n, float4* vclip)
+{
+    poly[0] = { c0, 1.f, 0.f, 0.f };
+    poly[1] = { c1, 0.f, 1.f, 0.f };
+    poly[2] = { c2, 0.f, 0.f, 1.f };
+    n = clip_polygon(poly, planes);
+    // Clipper.h:121-152: a vertex whose weight is exactly one on a source
+    // vertex is that source vertex (position and attributes); others are new.
+    const float4 src[3] = { c0, c1, c2 };
+    for (int j = 0; j < n; j++)
+    {
+        int s = -1;
+        if (poly[j].w0 == 1.0f) s = 0;
+        else if (poly[j].w1 == 1.0f) s = 1;
+        else if (poly[j].w2 == 1.0f) s = 2;
+        if (s >= 0)
+        {
+            poly[j].w0 = (s == 0) ? 1.f : 0.f;
+            poly[j].w1 = (s == 1) ? 1.f : 0.f;
+            poly[j].w2 = (s == 2) ? 1.f : 0.f;
+            vclip[j] = src[s];
+        }
+        else
+            vclip[j] = poly[j].p;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_setup(PassArgs a)
+{
+    const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = gi < a.total_tris;
+    const uint32_t lane = threadIdx.x & 31;
+
+    uint32_t fi = 0, tri = 0;
+    int nOut = 0;
+    bool clipped = false;
+    float4 c0 = {}, c1 = {}, c2 = {};
+    uint32_t planes = 0;
+    RTri t;
+    if (active)
+    {
+        fi = find_frame(a.frames, a.num_frames, gi, [](const FrameDesc& f) { return f.tri_base; });
+        const FrameDesc& f = a.frames[fi];
+        tri = gi - f.tri_base;
+        const uint32_t i0 = __ldg(f.indices + 3 * (size_t)tri);
+        const uint32_t i1 = __ldg(f.indices + 3 * (size_t)tri + 1);
+        const uint32_t i2 = __ldg(f.indices + 3 * (size_t)tri + 2);
+        if (i0 >= f.nv || i1 >= f.nv || i2 >= f.nv)
+        {
+            // device-resident index buffers are checked here instead of on the host
+            atomicOr(&a.status->error, 1u);  // EDXR_ERR_INVALID_ARG
+        }
+        else
+        {
+        c0 = a.clip[f.vtx_base + i0];
+        c1 = a.clip[f.vtx_base + i1];
+        c2 = a.clip[f.vtx_base + i2];
+        const uint32_t k0 = clip_code(c0), k1 = clip_code(c1), k2 = clip_code(c2);
+        if ((k0 | k1 | k2) == 0)
+        {
+            nOut = setup_triangle(f, c0, c1, c2, t) ? 1 : 0;
+        }
+        else if (!(k0 & k1 & k2))
+        {
+            clipped = true;
+            planes = (k0 ^ k1) | (k1 ^ k2) | (k2 ^ k0);
+            PolyVert poly[kMaxPolygon];
+            float4 vc[kMaxPolygon];
+            int n;
+            clip_triangle(f, c0, c1, c2, planes, poly, n, vc);
+            for (int k = 2; k < n; k++)
+            {
+                RTri tmp;
+                nOut += setup_triangle(f, vc[0], vc[k - 1], vc[k], tmp) ? 1 : 0;
+            }
+        }
+        }
+    }
+    // warp-aggregated append
+    int incl = nOut;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total > 0)
+        base = atomicAdd(&a.counters[0], (uint32_t)total);
+    base = __shfl_sync(0xffffffffu, base, 31) + (uint32_t)(incl - nOut);
+    if (nOut == 0)
+        return;
+    if (base + (uint32_t)nOut > a.rtri_capacity)
+    {
+        atomicOr(&a.status->overflow, 2u);
+        return;
+    }
+    if (!clipped)
+    {
+        t.order = tri << 4;
+        t.meta |= fi << 12;
+        t.poly = kUnclipped;
+        a.rtris[base] = t;
+        return;
+    }
+    const FrameDesc& f = a.frames[fi];
+    PolyVert poly[kMaxPolygon];
+    float4 vc[kMaxPolygon];
+    int n;
+    clip_triangle(f, c0, c1, c2, planes, poly, n, vc);
+    const uint32_t pi = atomicAdd(&a.counters[1], 1u);
+    if (pi >= a.poly_capacity)
+    {
+        atomicOr(&a.status->overflow, 4u);
+        return;
+    }
+    ClipPoly& P = a.polys[pi];
+    for (int j = 0; j < n; j++)
+    {
+        P.w[j][0] = poly[j].w0;
+        P.w[j][1] = poly[j].w1;
+        P.w[j][2] = poly[j].w2;
+    }
+    P.n = (uint32_t)n;
+    uint32_t out = base;
+    for (int k = 2; k < n; k++)
+    {
+        RTri tk;
+        if (!setup_triangle(f, vc[0], vc[k - 1], vc[k], tk))
+            continue;
+        tk.order = (tri << 4) | (uint32_t)(k - 2);
+        tk.meta |= fi << 12;
+        tk.poly = (pi << 4) | (uint32_t)k;
+        a.rtris[out++] = tk;
+    }
+}
+
+// -------------------------------------------------------------------------
+// Binning.  Phase 0 counts the non-rejected (triangle, tile) pairs per tile,
+// phase 1 writes entries (raster triangle << 2 | decision).  Triangles with
+// more than kBigTiles candidate tiles are binned by a whole block each.
+template <int Phase>
+__device__ __forceinline__ void bin_tile(const PassArgs& a, const FrameDesc& f, uint32_t ri, const RTri& t,
+                                         const Edges& e, const BinGeom& g, int tx, int ty)
+{
+    const uint32_t d = tile_decision(t, e, g, f, tx, ty);
+    if (!d)
+        return;
+    const uint32_t tile = f.tile_base + (uint32_t)(ty * f.tdx + tx);
+    if (Phase == 0)
+    {
+        atomicAdd(&a.tile_count[tile], 1u);
+    }
+    else
+    {
+        const uint64_t pos = (uint64_t)a.tile_offset[tile] + atomicAdd(&a.tile_cursor[tile], 1u);
+        if (pos < a.bin_capacity)
+            a.bins[pos] = (ri << 2) | d;
+    }
+}
+
+template <int Phase>
+__global__ void __launch_bounds__(256) k_bin(PassArgs a)
+{
+    const uint32_t n = *(volatile uint32_t*)&a.counters[0];
+    const uint32_t nr = min(n, a.rtri_capacity);
+    for (uint32_t ri = blockIdx.x * blockDim.x + threadIdx.x; ri < nr; ri += gridDim.x * blockDim.x)
+    {
+        const RTri t = a.rtris[ri];
+        const FrameDesc& f = a.frames[t.meta >> 12];
+        const BinGeom g = bin_geom(t, f);
+        const int nx = g.t16x1 - g.t16x0 + 1, ny = g.t16y1 - g.t16y0 + 1;
+        if (nx <= 0 || ny <= 0)
+            continue;
+        if (nx * ny > kBigTiles)
+        {
+            if (Phase == 0)
+            {
+                const uint32_t b = atomicAdd(&a.counters[2], 1u);
+                if (b < a.big_capacity)
+                    a.big_list[b] = ri;
+            }
+            continue;
+        }
+        const Edges e = tri_edges(t);
+        for (int ty = g.t16y0; ty <= g.t16y1; ty++)
+            for (int tx = g.t16x0; tx <= g.t16x1; tx++)
+                bin_tile<Phase>(a, f, ri, t, e, g, tx, ty);
+    }
+}
+
+template <int Phase>
+__global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
+{
+    const uint32_t nb = min(*(volatile uint32_t*)&a.counters[2], a.big_capacity);
+    for (uint32_t b = blockIdx.x; b < nb; b += gridDim.x)
+    {
+        const uint32_t ri = a.big_list[b];
+        const RTri t = a.rtris[ri];
+        const FrameDesc& f = a.frames[t.meta >> 12];
+        const BinGeom g = bin_geom(t, f);
+        const Edges e = tri_edges(t);
+        const int nx = g.t16x1 - g.t16x0 + 1, ny = g.t16y1 - g.t16y0 + 1;
+        for (int j = threadIdx.x; j < nx * ny; j += blockDim.x)
+            bin_tile<Phase>(a, f, ri, t, e, g, g.t16x0 + j % nx, g.t16y0 + j / nx);
+    }
+}
+
+// -------------------------------------------------------------------------
+// Exclusive scan of the per-tile counts, each rounded up to a multiple of 4
+// entries so every bin starts on a 16-byte boundary.
+__device__ __forceinline__ uint32_t padded(uint32_t c) { return (c + 3u) & ~3u; }
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_blocks(PassArgs a, uint32_t* block_sums)
+{
+    __shared__ uint32_t warp_sums[kScanThreads / 32];
+    const uint32_t base = blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems], s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++)
+    {
+        const uint32_t i = base + k;
+        v[k] = (i < a.total_tiles) ? padded(a.tile_count[i]) : 0u;
+        s += v[k];
+    }
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += t;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0)
+    {
+        uint32_t w = warp_sums[lane];
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= (uint32_t)o) wi += t;
+        }
+        warp_sums[lane] = wi - w;
+        if (lane == 31) block_sums[blockIdx.x] = wi;
+    }
+    __syncthreads();
+    uint32_t run = warp_sums[warp] + incl - s;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++)
+    {
+        const uint32_t i = base + k;
+        if (i < a.total_tiles) a.tile_offset[i] = run;
+        run += v[k];
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_spine(uint32_t* block_sums, uint32_t nblocks)
+{
+    // single block; nblocks <= 1024 * 4
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t v[4], s = 0;
+    for (int k = 0; k < 4; k++)
+    {
+        const uint32_t i = threadIdx.x * 4 + k;
+        v[k] = i < nblocks ? block_sums[i] : 0u;
+        s += v[k];
+    }
+    uint32_t incl = s;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += t;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0)
+    {
+        const uint32_t w = warp_sums[lane];
+        uint32_t wi = w;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= (uint32_t)o) wi += t;
+        }
+        warp_sums[lane] = wi - w;
+    }
+    __syncthreads();
+    uint32_t run = warp_sums[warp] + incl - s;
+    for (int k = 0; k < 4; k++)
+    {
+        const uint32_t i = threadIdx.x * 4 + k;
+        if (i < nblocks) block_sums[i] = run;  // exclusive
+        run += v[k];
+    }
+    if (threadIdx.x == blockDim.x - 1)
+        block_sums[nblocks] = run;  // grand total
+}
+
+__global__ void k_scan_add(PassArgs a, const uint32_t* block_sums, uint32_t nblocks)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.total_tiles)
+        a.tile_offset[i] += block_sums[i / kScanBlock];
+    if (i == 0)
+    {
+        const uint64_t total = block_sums[nblocks];
+        a.tile_offset[a.total_tiles] = (uint32_t)total;
+        a.status->bins_needed = total;
+        a.status->raster_tris = a.counters[0];
+        a.status->clipped_polys = a.counters[1];
+        a.status->big_tris = a.counters[2];
+        if (a.counters[0] > a.rtri_capacity)
+            atomicOr(&a.status->overflow, 2u);
+        if (a.counters[1] > a.poly_capacity)
+            atomicOr(&a.status->overflow, 4u);
+        if (total > a.bin_capacity)
+            atomicOr(&a.status->overflow, 1u);
+        if (a.counters[2] > a.big_capacity)
+            atomicOr(&a.status->overflow, 8u);
+    }
+}
+
+// -------------------------------------------------------------------------
+// Raster: persistent blocks take 16x16 tiles from a queue.  Each thread owns
+// one pixel and keeps the winner of the reference's sequential depth test as
+// a key: (depth, submission order) — for LEQUAL the last fragment with the
+// smallest depth wins, for LESS the first — so the bin needs no ordering.
+struct __align__(16) StagedTri
+{
+    int A0, D0, K0, A1;    // e0 = A0*lx + D0*ly + K0 (with bias); l1 = A1*lx + D1*ly + K1 (no bias)
+    int D1, K1, A2, D2;
+    int K2;
+    uint32_t flags;        // region lx0|lx1<<5|ly0<<10|ly1<<15, accept<<20, bias1<<21, bias2<<22
+    float invDet, z0;
+    float z1, z2;
+    uint32_t rank;         // order + 1
+    uint32_t ri;           // raster triangle index
+};
+
+__device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uint32_t nr, int tileX, int tileY,
+                                          StagedTri& s)
+{
+    const uint32_t ri = entry >> 2;
+    if (ri >= nr)
+    {
+        // never written by a consistent pass; an empty region keeps it inert
+        s.flags = 16u | (16u << 10);
+        s.ri = kNoTriangle;
+        return;
+    }
+    const bool accept = (entry & 3u) == kDecisionAccept;
+    const RTri t = a.rtris[ri];
+    const Edges e = tri_edges(t);
+    // pixel (lx, ly) of the tile samples at (16*(16*tileX + lx) + 8, ...)
+    const int ox = (tileX << 8) + 8, oy = (tileY << 8) + 8;
+    int A[3], D[3], K[3], bias[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        const int n = (k + 1) % 3;
+        bias[k] = tl_pixel(e.vx[k], e.vy[k], e.vx[n], e.vy[n]);
+        A[k] = wmul(16, e.B[k]);
+        D[k] = wmul(16, e.C[k]);
+        K[k] = wadd(wmul(e.B[k], wsub(ox, e.vx[k])), wmul(e.C[k], wsub(oy, e.vy[k])));
+    }
+    s.A0 = A[0]; s.D0 = D[0]; s.K0 = wadd(K[0], bias[0]);
+    // the barycentric numerators of RasterTriangle.h:335-336 are edges 1
+    // and 2 measured from v2, equal to the unbiased edge values
+    s.A1 = A[1]; s.D1 = D[1]; s.K1 = K[1];
+    s.A2 = A[2]; s.D2 = D[2]; s.K2 = K[2];
+    int lx0 = 0, lx1 = 15, ly0 = 0, ly1 = 15;
+    if (!accept)
+    {
+        const int bbx0 = min(t.v0x, min(t.v1x, t.v2x)) >> 4, bbx1 = max(t.v0x, max(t.v1x, t.v2x)) >> 4;
+        const int bby0 = min(t.v0y, min(t.v1y, t.v2y)) >> 4, bby1 = max(t.v0y, max(t.v1y, t.v2y)) >> 4;
+        lx0 = max(0, (bbx0 & ~1) - (tileX << 4));
+        lx1 = min(15, (bbx1 | 1) - (tileX << 4));
+        ly0 = max(0, (bby0 & ~1) - (tileY << 4));
+        ly1 = min(15, (bby1 | 1) - (tileY << 4));
+        if (lx1 < lx0 || ly1 < ly0) { lx0 = 16; lx1 = 0; ly0 = 16; ly1 = 0; }
+    }
+    s.flags = (uint32_t)lx0 | ((uint32_t)lx1 << 5) | ((uint32_t)ly0 << 10) | ((uint32_t)ly1 << 15) |
+              (accept ? (1u << 20) : 0u) | (bias[1] ? (1u << 21) : 0u) | (bias[2] ? (1u << 22) : 0u);
+    s.invDet = t.invDet;
+    s.z0 = t.z0; s.z1 = t.z1; s.z2 = t.z2;
+    s.rank = t.order + 1u;
+    s.ri = ri;
+}
+
+__global__ void __launch_bounds__(kRasterThreads) k_raster(PassArgs a)
+{
+    __shared__ StagedTri st[kRasterThreads];
+    __shared__ uint32_t s_tile;
+    const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
+    const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+            s_tile = atomicAdd(&a.counters[3], 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        __syncthreads();
+        if (tile >= a.total_tiles)
+            break;
+        const uint32_t fi = find_frame(a.frames, a.num_frames, tile, [](const FrameDesc& f) { return f.tile_base; });
+        const FrameDesc& f = a.frames[fi];
+        const uint32_t lt = tile - f.tile_base;
+        const int tileX = (int)(lt % (uint32_t)f.tdx), tileY = (int)(lt / (uint32_t)f.tdx);
+        const bool less = f.depth_func == 1;
+        uint32_t count = a.tile_count[tile];
+        const uint32_t start = a.tile_offset[tile];
+        if ((uint64_t)start + count > a.bin_capacity)
+            count = 0;  // overflowed frame: rendered again by the host
+
+        // best = (depth key << 32) | (LEQUAL: ~rank, LESS: rank); clear depth 1.0
+        uint64_t best = ((uint64_t)0xBF800000u << 32) | (less ? 0u : 0xFFFFFFFFu);
+        uint32_t bestRi = kNoTriangle;
+
+        for (uint32_t c = 0; c < count; c += kRasterThreads)
+        {
+            const uint32_t m = min((uint32_t)kRasterThreads, count - c);
+            if (threadIdx.x < m)
+                stage_tri(a, a.bins[start + c + threadIdx.x], nr, tileX, tileY, st[threadIdx.x]);
+            __syncthreads();
+            for (uint32_t j = 0; j < m; j++)
+            {
+                const uint32_t fl = st[j].flags;
+                const int lx0 = fl & 31, lx1 = (fl >> 5) & 31, ly0 = (fl >> 10) & 31, ly1 = (fl >> 15) & 31;
+                if (lx < lx0 || lx > lx1 || ly < ly0 || ly > ly1)
+                    continue;
+                const StagedTri& s = st[j];
+                const int l1 = wadd(wadd(wmul(s.A1, lx), wmul(s.D1, ly)), s.K1);
+                const int l2 = wadd(wadd(wmul(s.A2, lx), wmul(s.D2, ly)), s.K2);
+                if (!(fl & (1u << 20)))
+                {
+                    const int e0 = wadd(wadd(wmul(s.A0, lx), wmul(s.D0, ly)), s.K0);
+                    const int e1 = wadd(l1, (fl & (1u << 21)) ? -1 : 0);
+                    const int e2 = wadd(l2, (fl & (1u << 22)) ? -1 : 0);
+                    if ((e0 | e1 | e2) < 0)
+                        continue;
+                }
+                // TriangleSSE::CalcBarycentricCoord / GetDepth (RasterTriangle.h:324-337)
+                const float L0 = fmul(__int2float_rn(l1), s.invDet);
+                const float L1 = fmul(__int2float_rn(l2), s.invDet);
+                const float L2 = fsub(fsub(1.0f, L0), L1);
+                const float d = fadd(fadd(fmul(L0, s.z0), fmul(L1, s.z1)), fmul(L2, s.z2));
+                if (d != d)
+                    continue;
+                const uint64_t key = ((uint64_t)depth_key(d) << 32) | (less ? s.rank : ~s.rank);
+                if (key < best)
+                {
+                    best = key;
+                    bestRi = s.ri;
+                }
+            }
+            __syncthreads();
+        }
+
+        // epilogue: shade the winner, one write of colour, depth and id
+        const int px = (tileX << 4) + lx, py = (tileY << 4) + ly;
+        if (px < f.width && py < f.height)
+        {
+            const uint64_t o = f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px;
+            if (bestRi != kNoTriangle)
+            {
+                const RTri t = a.rtris[bestRi];
+                const Edges e = tri_edges(t);
+                const int cx = (px << 4) + 8, cy = (py << 4) + 8;
+                const int n1 = wadd(wmul(e.B[1], wsub(cx, t.v2x)), wmul(e.C[1], wsub(cy, t.v2y)));
+                const int n2 = wadd(wmul(e.B[2], wsub(cx, t.v2x)), wmul(e.C[2], wsub(cy, t.v2y)));
+                const float L0 = fmul(__int2float_rn(n1), t.invDet);
+                const float L1 = fmul(__int2float_rn(n2), t.invDet);
+                const float L2 = fsub(fsub(1.0f, L0), L1);
+                const float d = fadd(fadd(fmul(L0, t.z0), fmul(L1, t.z1)), fmul(L2, t.z2));
+                const float3 c = shade_fragment(f, t, a.polys, L0, L1);
+                a.color[o] = make_float4(c.x, c.y, c.z, 1.0f);
+                a.depth[o] = d;
+                a.tri_id[o] = t.order >> 4;
+            }
+            else
+            {
+                a.color[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+                a.depth[o] = 1.0f;
+                a.tri_id[o] = kNoTriangle;
+            }
+        }
+    }
+}
+
+// -------------------------------------------------------------------------
+// Renderer::GetBackBuffer compatibility: RGBA8, bottom-up (FrameBuffer.cpp:41).
+__global__ void k_back_buffer(const float4* color, uchar4* out, int width, int height)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= width * height)
+        return;
+    const int x = i % width, y = i / width;
+    const float4 c = color[i];
+    auto b = [](float v) -> unsigned char {
+        v = fminf(fmaxf(v, 0.0f), 1.0f);
+        return (unsigned char)(v * 255.0f + 0.5f);
+    };
+    const bool covered = c.w > 0.0f;
+    out[(size_t)(height - 1 - y) * width + x] = make_uchar4(b(c.x), b(c.y), b(c.z), covered ? 255 : 0);
+}
+
+// -------------------------------------------------------------------------
+
+
+static int raster_blocks(int sms)
+{
+    static int per_sm = 0;
+    if (!per_sm)
+    {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster, kRasterThreads, 0) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+    }
+    return sms * per_sm;
+}
+
+void prepare_kernels()
+{
+    raster_blocks(1);
+}
+
+cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
+{
+    const int sms = a.num_sms > 0 ? a.num_sms : 148;
+    const uint32_t nscan = (a.total_tiles + kScanBlock - 1) / kScanBlock;
+    uint32_t* block_sums = a.tile_cursor + a.total_tiles + 1;  // scratch after the cursors
+    auto mark = [&](int i) {
+        if (ev) cudaEventRecord(ev[i], s);
+    };
+    mark(0);
+    k_clear<<<(a.total_tiles + 1 + 255) / 256 + 1, 256, 0, s>>>(a);
+    if (a.total_vertices)
+        k_vertex<<<(a.total_vertices + 255) / 256, 256, 0, s>>>(a);
+    mark(1);
+    if (a.total_tris)
+        k_setup<<<(a.total_tris + 255) / 256, 256, 0, s>>>(a);
+    mark(2);
+    k_bin<0><<<sms * 8, 256, 0, s>>>(a);
+    k_bin_big<0><<<sms * 4, 256, 0, s>>>(a);
+    mark(3);
+    k_scan_blocks<<<nscan, kScanThreads, 0, s>>>(a, block_sums);
+    k_scan_spine<<<1, 1024, 0, s>>>(block_sums, nscan);
+    k_scan_add<<<(a.total_tiles + 255) / 256 + 1, 256, 0, s>>>(a, block_sums, nscan);
+    mark(4);
+    k_bin<1><<<sms * 8, 256, 0, s>>>(a);
+    k_bin_big<1><<<sms * 4, 256, 0, s>>>(a);
+    mark(5);
+    k_raster<<<raster_blocks(sms), kRasterThreads, 0, s>>>(a);
+    mark(6);
+    return cudaGetLastError();
+}
+
+int kernels_per_pass(const PassArgs& a)
+{
+    return 9 + (a.total_vertices ? 1 : 0) + (a.total_tris ? 1 : 0);
+}
+
+cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s)
+{
+    const int n = width * height;
+    k_back_buffer<<<(n + 255) / 256, 256, 0, s>>>(color, reinterpret_cast<uchar4*>(rgba8), width, height);
+    return cudaGetLastError();
+}
+
+}  // namespace edxr

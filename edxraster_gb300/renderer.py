@@ -1,0 +1,298 @@
+"""Python mirror of EDXRaster's Renderer (EDXRaster/Core/Renderer.h:15-59) over
+the C ABI of include/edxr.h.
+
+Method names and meaning follow the reference: Initialize, Resize,
+SetTransform, RenderMesh, WriteFrameToFile, GetBackBuffer, SetMSAAMode,
+SetTextureFilter, SetHierarchicalRasterize, SetWriteFrames.  Where the
+reference returns nothing and ignores errors, these raise ``EdxrError``.
+Extra methods expose what the GPU build adds: the depth function, pixel-shader
+selection, float outputs, the batched form and the adjoint.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _lib
+from ._lib import EdxrError  # noqa: F401  (re-exported)
+
+DEPTH_LEQUAL, DEPTH_LESS = 0, 1
+PS_BLINN_PHONG, PS_BLINN_PHONG_REFERENCE, PS_LAMBERTIAN_ALBEDO, PS_LAMBERTIAN = 0, 1, 2, 3
+
+
+def _f16(m):
+    m = np.ascontiguousarray(np.asarray(m, np.float32).reshape(16))
+    return (ctypes.c_float * 16)(*m)
+
+
+class DeviceMesh:
+    """A mesh resident in device memory (torch CUDA tensors), passed by pointer."""
+
+    def __init__(self, positions, indices, normals=None, albedo=None, uvs=None):
+        import torch
+        dev = positions.device
+
+        def prep(t, dtype, cols):
+            if t is None:
+                return None
+            if not isinstance(t, torch.Tensor):
+                t = torch.from_numpy(np.ascontiguousarray(t))
+            t = t.to(device=dev, dtype=dtype).contiguous()
+            assert t.dim() == 2 and t.shape[1] == cols
+            return t
+
+        self.positions = prep(positions, torch.float32, 3)
+        self.indices = prep(indices, torch.int32, 3)
+        self.normals = prep(normals, torch.float32, 3)
+        self.albedo = prep(albedo, torch.float32, 3)
+        self.uvs = prep(uvs, torch.float32, 2)
+
+    @classmethod
+    def from_mesh(cls, mesh, device="cuda"):
+        import torch
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)  # noqa: E731
+        return cls(t(mesh.positions), t(mesh.indices.astype(np.int32)), t(mesh.normals), t(mesh.albedo), t(mesh.uvs))
+
+    @property
+    def nv(self):
+        return int(self.positions.shape[0])
+
+    @property
+    def nt(self):
+        return int(self.indices.shape[0])
+
+    def abi(self) -> _lib.Mesh:
+        p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        return _lib.Mesh(p(self.positions), 12, p(self.normals), 12, p(self.uvs), 8, p(self.albedo), 12,
+                         p(self.indices), self.nv, self.nt, _lib.MEMORY_DEVICE)
+
+
+class HostMesh:
+    """A mesh in host memory (numpy), copied to the device by every render call."""
+
+    def __init__(self, mesh, pinned=False):
+        self._keep = []
+
+        def prep(a, dtype):
+            a = np.ascontiguousarray(a, dtype)
+            if pinned:
+                import torch
+                t = torch.from_numpy(a).pin_memory()
+                self._keep.append(t)
+                return t.numpy()
+            return a
+
+        self.positions = prep(mesh.positions, np.float32)
+        self.normals = prep(mesh.normals, np.float32)
+        self.albedo = prep(mesh.albedo, np.float32)
+        self.uvs = prep(mesh.uvs, np.float32)
+        self.indices = prep(mesh.indices, np.uint32)
+        self.nv, self.nt = int(self.positions.shape[0]), int(self.indices.shape[0])
+
+    def nbytes(self) -> int:
+        return sum(a.nbytes for a in (self.positions, self.normals, self.albedo, self.uvs, self.indices))
+
+    def abi(self) -> _lib.Mesh:
+        return _lib.Mesh(self.positions.ctypes.data, 12, self.normals.ctypes.data, 12, self.uvs.ctypes.data, 8,
+                         self.albedo.ctypes.data, 12, self.indices.ctypes.data, self.nv, self.nt, _lib.MEMORY_HOST)
+
+
+def _as_abi_mesh(mesh):
+    if isinstance(mesh, (DeviceMesh, HostMesh)):
+        return mesh, mesh.abi()
+    hm = HostMesh(mesh)
+    return hm, hm.abi()
+
+
+class Renderer:
+    """GPU renderer with the reference's public interface."""
+
+    def __init__(self, device: int = 0, stream=None):
+        self._lib = _lib.load()
+        self._h = ctypes.c_void_p()
+        self._device = device
+        self._stream = stream
+        self._width = self._height = 0
+        self._state = _lib.State(DEPTH_LEQUAL, 1, 0, 0)
+        self._write_frames = False
+        self._frame = 0
+        self._keep = None
+
+    # -- lifetime -----------------------------------------------------------
+    def Initialize(self, width: int, height: int):
+        """Renderer::Initialize (Renderer.cpp:22-62)."""
+        if self._h:
+            self.Resize(width, height)
+            return
+        stream = self._stream
+        if stream is None:
+            import torch
+            stream = torch.cuda.Stream(device=self._device)
+            self._stream = stream
+        handle = getattr(stream, "cuda_stream", stream)
+        init = _lib.Init(width, height, handle, self._device)
+        _lib.check(self._lib.edxr_create(ctypes.byref(self._h), ctypes.byref(init)))
+        self._width, self._height = width, height
+        _lib.check(self._lib.edxr_set_state(self._h, ctypes.byref(self._state)))
+
+    def close(self):
+        if self._h:
+            self._lib.edxr_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        return self._stream
+
+    # -- reference interface ---------------------------------------------------
+    def Resize(self, width: int, height: int):
+        """Renderer::Resize (Renderer.cpp:64-83)."""
+        _lib.check(self._lib.edxr_resize(self._h, width, height))
+        self._width, self._height = width, height
+
+    def SetTransform(self, model_view, proj, to_raster):
+        """Renderer::SetTransform (Renderer.cpp:85-92)."""
+        self._mv, self._proj, self._raster = _f16(model_view), _f16(proj), _f16(to_raster)
+        _lib.check(self._lib.edxr_set_transform(self._h, ctypes.addressof(self._mv), ctypes.addressof(self._proj),
+                                                ctypes.addressof(self._raster)))
+
+    def SetMSAAMode(self, msaa_count_log2: int):
+        """Renderer::SetMSAAMode (Renderer.cpp:94-98); only 0 is provided."""
+        self._state.msaa_log2 = msaa_count_log2
+        try:
+            _lib.check(self._lib.edxr_set_state(self._h, ctypes.byref(self._state)))
+        finally:
+            self._state.msaa_log2 = 0
+
+    def SetTextureFilter(self, texture_filter: int):
+        """Renderer::SetTextureFilter (Renderer.h:48); stored, no texture sampling here."""
+        self._state.texture_filter = int(texture_filter)
+        _lib.check(self._lib.edxr_set_state(self._h, ctypes.byref(self._state)))
+
+    def SetHierarchicalRasterize(self, h: bool):
+        """Renderer::SetHierarchicalRasterize (Renderer.h:49)."""
+        self._state.hierarchical = 1 if h else 0
+        _lib.check(self._lib.edxr_set_state(self._h, ctypes.byref(self._state)))
+
+    def SetWriteFrames(self, wf: bool):
+        """Renderer::SetWriteFrames (Renderer.h:50)."""
+        self._write_frames = bool(wf)
+
+    def SetDepthFunc(self, func: int):
+        self._state.depth_func = int(func)
+        _lib.check(self._lib.edxr_set_state(self._h, ctypes.byref(self._state)))
+
+    def SetPixelShader(self, kind: int, light=(1.0, 1.0, -1.0), ks: float = 0.5, shininess: float = 32.0):
+        p = _lib.ShaderParams((ctypes.c_float * 3)(*[float(x) for x in light]), float(ks), float(shininess))
+        _lib.check(self._lib.edxr_set_shader(self._h, 0, int(kind), ctypes.byref(p)))
+
+    def RenderMesh(self, mesh, synchronize: bool = True):
+        """Renderer::RenderMesh (Renderer.cpp:100-118): clear and render one mesh."""
+        keep, m = _as_abi_mesh(mesh)
+        self._keep = (keep, m)
+        _lib.check(self._lib.edxr_render(self._h, ctypes.byref(m)))
+        if synchronize:
+            self.Synchronize()
+        self._frame += 1
+        if self._write_frames:
+            self.WriteFrameToFile()
+
+    def Synchronize(self):
+        _lib.check(self._lib.edxr_synchronize(self._h))
+
+    def GetBackBuffer(self) -> np.ndarray:
+        """Renderer::GetBackBuffer (Renderer.cpp:360-363): RGBA8, bottom-up rows."""
+        p = ctypes.c_void_p()
+        _lib.check(self._lib.edxr_get_back_buffer(self._h, ctypes.byref(p)))
+        buf = (ctypes.c_uint8 * (4 * self._width * self._height)).from_address(p.value)
+        return np.frombuffer(buf, np.uint8).reshape(self._height, self._width, 4).copy()
+
+    def WriteFrameToFile(self, directory: str = "Frames"):
+        """Renderer::WriteFrameToFile (Renderer.cpp:352-358): a BMP of the back buffer."""
+        os.makedirs(directory, exist_ok=True)
+        img = self.GetBackBuffer()  # bottom-up rows, which is BMP's native row order
+        h, w = img.shape[:2]
+        bgra = img[..., [2, 1, 0, 3]].tobytes()
+        hdr = b"BM" + (54 + len(bgra)).to_bytes(4, "little") + b"\0\0\0\0" + (54).to_bytes(4, "little")
+        dib = (40).to_bytes(4, "little") + w.to_bytes(4, "little") + h.to_bytes(4, "little", signed=True) + \
+            (1).to_bytes(2, "little") + (32).to_bytes(2, "little") + b"\0" * 24
+        path = os.path.join(directory, "Frame%05d.bmp" % self._frame)
+        with open(path, "wb") as fh:
+            fh.write(hdr + dib + bgra)
+        return path
+
+    # -- outputs -------------------------------------------------------------
+    def ReadOutputs(self):
+        """Host copies of the last frame: colour (H,W,4) f32, depth (H,W) f32, triangle id (H,W) u32."""
+        W, H = self._width, self._height
+        color = np.empty((H, W, 4), np.float32)
+        depth = np.empty((H, W), np.float32)
+        tid = np.empty((H, W), np.uint32)
+        _lib.check(self._lib.edxr_read_outputs(self._h, color.ctypes.data, depth.ctypes.data, tid.ctypes.data))
+        return color, depth, tid
+
+    def DeviceOutputs(self) -> _lib.Outputs:
+        o = _lib.Outputs()
+        _lib.check(self._lib.edxr_get_outputs(self._h, ctypes.byref(o)))
+        return o
+
+    def Stats(self) -> _lib.Stats:
+        s = _lib.Stats()
+        _lib.check(self._lib.edxr_get_stats(self._h, ctypes.byref(s)))
+        return s
+
+    STAGES = ("clear+vertex", "clip+setup", "bin count", "bin scan", "bin scatter", "raster+shade")
+
+    def SetProfiling(self, enable: bool):
+        _lib.check(self._lib.edxr_set_profiling(self._h, 1 if enable else 0))
+
+    def StageTimes(self) -> dict:
+        """Milliseconds per stage of the last pass (profiling must be on)."""
+        ms = (ctypes.c_float * 8)()
+        n = ctypes.c_uint32(8)
+        _lib.check(self._lib.edxr_get_stage_times(self._h, ms, ctypes.byref(n)))
+        return {self.STAGES[i]: float(ms[i]) for i in range(n.value)}
+
+    # -- batched form ----------------------------------------------------------
+    def RenderBatched(self, meshes, views, width: int, height: int, synchronize: bool = True):
+        """Render every (mesh, view) pair in one pass; views are scenes.View with a .mesh index."""
+        keeps, abis = [], []
+        for m in meshes:
+            k, a = _as_abi_mesh(m)
+            keeps.append(k)
+            abis.append(a)
+        marr = (_lib.Mesh * len(abis))(*abis)
+        varr = (_lib.View * len(views))()
+        for i, v in enumerate(views):
+            varr[i].mesh = v.mesh
+            varr[i].mv = _f16(v.mv)
+            varr[i].proj = _f16(v.proj)
+            varr[i].raster = _f16(v.raster)
+            varr[i].shading = _lib.ShaderParams((ctypes.c_float * 3)(*[float(x) for x in v.light]), v.ks, v.shininess)
+            varr[i].ps_kind = v.shader
+            varr[i].depth_func = v.depth_func
+        self._keep = (keeps, marr, varr)
+        _lib.check(self._lib.edxr_render_batched(self._h, marr, len(abis), varr, len(views), width, height))
+        if synchronize:
+            self.Synchronize()
+
+    def BatchOutputs(self) -> _lib.BatchOutputs:
+        o = _lib.BatchOutputs()
+        _lib.check(self._lib.edxr_get_batch_outputs(self._h, ctypes.byref(o)))
+        return o
+
+
+def configure(r: Renderer, view, hierarchical: bool = True):
+    """Apply a scenes.View (camera, shader, depth function) to a renderer."""
+    r.SetTransform(view.mv, view.proj, view.raster)
+    r.SetPixelShader(view.shader, view.light, view.ks, view.shininess)
+    r.SetDepthFunc(view.depth_func)
+    r.SetHierarchicalRasterize(hierarchical)

@@ -115,7 +115,10 @@ static unsigned clip_code(vec4f v)
 }
 
 typedef struct { vec4f pos; float w[3]; } pvert;
-typedef struct { pvert v[16]; int n; } polygon;
+/* The reference's polygon is a growable Array (Clipper.h:26); 64 slots are
+ * far more than the 9 exact arithmetic allows. */
+#define MAX_POLY 64
+typedef struct { pvert v[MAX_POLY]; int n; } polygon;
 
 static int plane_inside(int plane, vec4f v)
 {
@@ -184,6 +187,8 @@ static void clip_by_plane(int plane, const polygon* in, polygon* out)
         if (i1 == in->n) i1 = 0;
         const pvert* v0 = &in->v[i];
         const pvert* v1 = &in->v[i1];
+        if (out->n + 2 > MAX_POLY)
+            break;
         if (plane_inside(plane, v0->pos))
         {
             if (plane_inside(plane, v1->pos))
@@ -397,7 +402,7 @@ static int stage_clip(frame* f)
                     poly.v[k].w[k] = 1.0f;
                 }
                 clip_polygon(&poly, (c0 ^ c1) | (c1 ^ c2) | (c2 ^ c0));
-                uint32_t ids[16];
+                uint32_t ids[MAX_POLY];
                 for (int j = 0; j < poly.n; j++)
                 {
                     const float* w = poly.v[j].w;

@@ -1,0 +1,88 @@
+"""The CPU oracle (C restatement) against the reference's own pipeline.
+
+The golden fixtures hold what the reference's Renderer (its Core sources
+compiled unmodified against oracle/shim) produced; the oracle must match them
+bit for bit: winning triangle, depth buffer, barycentrics.  When the
+reference sources are present, further seeded scenes are compared live.
+"""
+import numpy as np
+import pytest
+
+from edxraster_gb300 import scenes
+from oracle import pyoracle
+from _scenes import golden_names, load_golden, mismatch_report
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_oracle_matches_golden(name):
+    sc, hier, exp = load_golden(name)
+    o = pyoracle.render_oracle(sc.mesh, sc.view, hierarchical=hier, depth_func=scenes.DEPTH_LEQUAL, threads=2)
+    assert not mismatch_report("id", o["id"], exp["id"])
+    assert not mismatch_report("depth", o["depth"].view(np.uint32), exp["depth_bits"])
+    covered = exp["id"] != 0xFFFFFFFF
+    assert np.array_equal(o["lambda0"].view(np.uint32)[covered], exp["lambda0_bits"][covered])
+    assert np.array_equal(o["lambda1"].view(np.uint32)[covered], exp["lambda1_bits"][covered])
+    assert o["fragments"] == exp["fragments"]
+
+
+def _live_cases():
+    yield scenes.small_random_scene(11, 80, 64, ntris=120), True
+    yield scenes.small_random_scene(12, 80, 64, ntris=120), False
+    yield scenes.small_random_scene(13, 64, 48, ntris=200, clip_heavy=False), True
+    yield scenes.stress_scene(3000, 320, 240, seed=3, max_area=5e3), True
+    yield scenes.terrain_scene(40, 160, 96, seed=5), True
+    yield scenes.sphere_scene(200, 120, slices=12, stacks=9), True
+
+
+@pytest.mark.parametrize("case", range(6))
+def test_oracle_matches_reference_live(case):
+    if pyoracle.reference_lib() is None:
+        pytest.skip("reference sources not available here")
+    sc, hier = list(_live_cases())[case]
+    r = pyoracle.render_reference(sc.mesh, sc.view, hierarchical=hier)
+    o = pyoracle.render_oracle(sc.mesh, sc.view, hierarchical=hier, depth_func=scenes.DEPTH_LEQUAL, threads=2)
+    assert not mismatch_report("id", o["id"], r["id"])
+    assert not mismatch_report("depth", o["depth"].view(np.uint32), r["depth"].view(np.uint32))
+    assert o["fragments"] == r["fragments"]
+
+
+def test_less_differs_only_on_ties():
+    """LESS keeps the first of equal-depth fragments, LEQUAL the last; the
+    stress scene has exact duplicates, so some pixels must differ and every
+    differing pixel must carry the same depth."""
+    sc = scenes.stress_scene(4000, 200, 160, seed=7, max_area=3e3, dup_fraction=0.2)
+    a = pyoracle.render_oracle(sc.mesh, sc.view, depth_func=scenes.DEPTH_LEQUAL, threads=2, with_color=False)
+    b = pyoracle.render_oracle(sc.mesh, sc.view, depth_func=scenes.DEPTH_LESS, threads=2, with_color=False)
+    diff = a["id"] != b["id"]
+    assert diff.any()
+    assert np.array_equal(a["depth"][diff], b["depth"][diff])
+
+
+def test_hierarchical_flag_does_not_change_coverage():
+    sc = scenes.stress_scene(2000, 256, 160, seed=9, max_area=1e4)
+    a = pyoracle.render_oracle(sc.mesh, sc.view, hierarchical=True, threads=2, with_color=False)
+    b = pyoracle.render_oracle(sc.mesh, sc.view, hierarchical=False, threads=2, with_color=False)
+    assert np.array_equal(a["id"], b["id"])
+    assert np.array_equal(a["depth"].view(np.uint32), b["depth"].view(np.uint32))
+
+
+def test_oracle_rejects_bad_indices():
+    sc = scenes.small_random_scene(1)
+    sc.mesh.indices = sc.mesh.indices.copy()
+    sc.mesh.indices[3, 1] = sc.mesh.nv + 5
+    with pytest.raises(RuntimeError):
+        pyoracle.render_oracle(sc.mesh, sc.view, threads=1)
+
+
+def test_shading_model_fp64_known_values():
+    """Head-on Blinn-Phong at one point: N = L = E = +z-facing."""
+    v = scenes.View(4, 4, np.eye(4, dtype=np.float32), np.eye(4, dtype=np.float32), np.eye(4, dtype=np.float32),
+                    np.array([0, 0, -1], np.float32), 0.5, 32.0)
+    b = np.array([1.0, 0.0, 0.0])
+    pos = np.zeros((3, 3))
+    nrm = np.tile([0.0, 0.0, -1.0], (3, 1))
+    alb = np.tile([0.25, 0.5, 1.0], (3, 1))
+    eye = np.array([0.0, 0.0, -5.0])
+    rgb = pyoracle.shade_fp64(v, b, pos, nrm, alb, eye)
+    diffuse = (1.0 + 0.2) * 3.0 / np.pi
+    assert np.allclose(rgb, alb[0] * diffuse + 0.5, rtol=0, atol=1e-12)
