@@ -77,7 +77,7 @@ void mat_mul(const float* A, const float* B, float* C)
 }
 
 // Eye position MV^-1 * 0 (Renderer.cpp:289) by Gauss-Jordan in double.
-bool eye_from_mv(const float* mv, float eye[3])
+bool eye_from_mv(const float* mv, double eye[3])
 {
     double a[4][8];
     for (int i = 0; i < 4; i++)
@@ -105,9 +105,9 @@ bool eye_from_mv(const float* mv, float eye[3])
         }
     }
     const double w = a[3][7];
-    eye[0] = (float)(a[0][7] / w);
-    eye[1] = (float)(a[1][7] / w);
-    eye[2] = (float)(a[2][7] / w);
+    eye[0] = a[0][7] / w;
+    eye[1] = a[1][7] / w;
+    eye[2] = a[2][7] / w;
     return true;
 }
 
@@ -223,14 +223,9 @@ edxr_status check_mesh(const edxr_mesh* m)
         return fail(EDXR_ERR_INVALID_ARG, "albedo stride below 12 bytes");
     if (m->uvs && m->uv_stride < 8)
         return fail(EDXR_ERR_INVALID_ARG, "uv stride below 8 bytes");
-    if (m->memory == EDXR_MEMORY_HOST)
-    {
-        // the reference asserts on index range (InputBuffer.h:177); check here
-        const uint64_t n = 3ull * m->num_triangles;
-        for (uint64_t i = 0; i < n; i++)
-            if (m->indices[i] >= m->num_vertices)
-                return fail(EDXR_ERR_INVALID_ARG, "vertex index out of range");
-    }
+    // Index range (the reference asserts it, InputBuffer.h:177) is checked by
+    // the setup kernel for host and device meshes alike; a bad index makes the
+    // frame fail with EDXR_ERR_INVALID_ARG at synchronisation.
     return EDXR_OK;
 }
 
@@ -294,8 +289,13 @@ void fill_frame(FrameDesc& f, const edxr_mesh& m, const Camera& cam, const Shadi
     f.hierarchical = hierarchical ? 1 : 0;
     mat_mul(cam.proj, cam.mv, f.mvp);
     std::memcpy(f.raster, cam.raster, sizeof(f.raster));
-    if (!eye_from_mv(cam.mv, f.eye))
-        f.eye[0] = f.eye[1] = f.eye[2] = 0.0f;
+    if (!eye_from_mv(cam.mv, f.eye_d))
+        f.eye_d[0] = f.eye_d[1] = f.eye_d[2] = 0.0;
+    for (int q = 0; q < 3; q++)
+    {
+        f.eye[q] = (float)f.eye_d[q];
+        f.light_raw[q] = sh.p.light[q];
+    }
     const double lx = sh.p.light[0], ly = sh.p.light[1], lz = sh.p.light[2];
     const double ln = std::sqrt(lx * lx + ly * ly + lz * lz);
     f.light[0] = (float)(lx / ln);
@@ -428,7 +428,9 @@ edxr_status sync_pass(edxr_renderer* r)
         if (st.error)
         {
             r->pending = false;
-            return fail((edxr_status)st.error, "device reported an error");
+            return fail((edxr_status)st.error, st.error == EDXR_ERR_INVALID_ARG
+                                                   ? "a triangle references a vertex index out of range"
+                                                   : "the device reported an error");
         }
         if (!st.overflow)
             break;

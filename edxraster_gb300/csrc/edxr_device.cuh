@@ -497,11 +497,56 @@ __device__ __forceinline__ float3 shade_model(const FrameDesc& f, float3 P, floa
     }
 }
 
+// BlinnPhongPixelShader as written (ks = 3, exponent 200, no clamp) amplifies
+// the error of N.H by ks*s*x^(s-1) = 600: FP32 unit vectors cannot hold N.H
+// to the ~5e-9 that 1e-5 of colour needs, so this shader interpolates and
+// shades in FP64.
+__device__ __noinline__ float3 shade_fragment_fp64(const FrameDesc& f, const RTri& t, const ClipPoly* polys,
+                                                   float l0, float l1)
+{
+    double b0 = l0, b1 = l1;
+    double b2 = 1.0 - b0 - b1;
+    b0 *= (double)t.invW0;
+    b1 *= (double)t.invW1;
+    b2 *= (double)t.invW2;
+    const double s = 1.0 / (b0 + b1 + b2);
+    b0 *= s;
+    b1 *= s;
+    b2 = 1.0 - b0 - b1;
+    const ShadeVerts v = shade_verts(f, t, polys);
+    double P[3], N[3];
+    const float* vp[3] = { &v.p[0].x, &v.p[1].x, &v.p[2].x };
+    const float* vn[3] = { &v.n[0].x, &v.n[1].x, &v.n[2].x };
+    for (int q = 0; q < 3; q++)
+    {
+        P[q] = b0 * vp[0][q] + b1 * vp[1][q] + b2 * vp[2][q];
+        N[q] = b0 * vn[0][q] + b1 * vn[1][q] + b2 * vn[2][q];
+    }
+    double inv = 1.0 / sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+    for (int q = 0; q < 3; q++) N[q] *= inv;
+    double L[3] = { f.light_raw[0], f.light_raw[1], f.light_raw[2] };
+    inv = 1.0 / sqrt(L[0] * L[0] + L[1] * L[1] + L[2] * L[2]);
+    for (int q = 0; q < 3; q++) L[q] *= inv;
+    double nl = L[0] * N[0] + L[1] * N[1] + L[2] * N[2];
+    if (nl < 0.0) nl = 0.0;
+    const double diffuse = (nl + 0.2) * 3.0 / 3.14159265358979323846;
+    double E[3] = { f.eye_d[0] - P[0], f.eye_d[1] - P[1], f.eye_d[2] - P[2] };
+    inv = 1.0 / sqrt(E[0] * E[0] + E[1] * E[1] + E[2] * E[2]);
+    double H[3];
+    for (int q = 0; q < 3; q++) H[q] = L[q] + E[q] * inv;
+    inv = 1.0 / sqrt(H[0] * H[0] + H[1] * H[1] + H[2] * H[2]);
+    const double nh = (N[0] * H[0] + N[1] * H[1] + N[2] * H[2]) * inv;
+    const float c = (float)(diffuse + (double)f.ks * pow(nh, (double)f.shininess));
+    return f3(c, c, c);
+}
+
 // Fragment::Interpolate (Shader.h:142-170) from the fragment's barycentrics,
 // then the shading model.
 __device__ __forceinline__ float3 shade_fragment(const FrameDesc& f, const RTri& t, const ClipPoly* polys,
                                                  float l0, float l1)
 {
+    if (f.ps_kind == 1)
+        return shade_fragment_fp64(f, t, polys, l0, l1);
     float b0 = l0, b1 = l1;
     float b2 = fsub(fsub(1.0f, b0), b1);
     b0 = fmul(b0, t.invW0);

@@ -49,6 +49,9 @@ struct FrameDesc
     float light[3];      // normalised light direction
     float ks, shininess;
     float ndc_from_raster[6];  // 2D affine inverse of the raster matrix (x, y rows)
+    float light_raw[3];        // light direction as given (FP64 shading normalises it)
+    float pad2;
+    double eye_d[3];           // eye position in double (FP64 shading)
 };
 
 // One triangle after clipping and setup (RasterTriangle, RasterTriangle.h:11-24),
