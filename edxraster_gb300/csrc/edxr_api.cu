@@ -26,6 +26,12 @@ edxr_status fail(edxr_status s, const std::string& msg)
     return s;
 }
 
+}  // namespace
+
+void edxr::record_error(const char* msg) { g_last_error = msg; }
+
+namespace {
+
 #define EDXR_CUDA(call)                                                                        \
     do {                                                                                       \
         cudaError_t e_ = (call);                                                               \

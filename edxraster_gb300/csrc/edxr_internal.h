@@ -122,6 +122,8 @@ constexpr int kStageEvents = 7;  // boundaries of the 6 timed stages
 // ev: NULL, or kStageEvents events recorded around the stages.
 cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev = nullptr);
 int kernels_per_pass(const PassArgs& a);
+// Sets the message edxr_last_error_string returns on this thread.
+void record_error(const char* msg);
 void prepare_kernels();
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s);
 cudaError_t launch_shade_visible(const PassArgs& a, float4* out, cudaStream_t s);

@@ -256,6 +256,29 @@ edxr_status edxr_shade_visible(edxr_renderer* r, const edxr_mesh* mesh, float* c
 edxr_status edxr_backward(edxr_renderer* r, const edxr_mesh* mesh, const float* grad_color,
                           const edxr_grads* grads);
 
+/* ---- rendering without device allocation ---------------------------------- */
+
+/* No counterpart in the reference.  One frame for callers that cannot
+ * allocate device memory: hosts that own all device memory and give the
+ * renderer a fixed budget (engines, plugin hosts), and latency-bound loops
+ * that must not call cudaMalloc / cudaFree, which synchronise the device.
+ * The caller passes the mesh (device memory), the camera, the state and the
+ * shader, and the three output images (device memory, width*height*4 floats,
+ * width*height floats, width*height u32).  Every intermediate buffer lives in
+ * one fixed file-scope device array (about 12 MiB, held by every GPU that
+ * loads the library until exit); nothing is allocated.  Limits: 65536
+ * vertices, 65536 triangles, 4096 pixels per side and 2^20 pixels; larger
+ * requests fail with EDXR_ERR_INVALID_ARG, and a frame whose bins or clipped
+ * polygons do not fit fails with EDXR_ERR_OVERFLOW.  The first call on a
+ * device looks the array up with cudaGetSymbolAddress: make it before any
+ * stream capture.  Calls share the array and keep its contents; calls whose
+ * GPU work overlaps race, so serialise them.  The call waits for the frame
+ * on `stream` (a cudaStream_t, NULL = legacy default stream). */
+edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const float proj[16],
+                                const float raster[16], const edxr_state* state, int ps_kind,
+                                const edxr_shader_params* params, uint32_t width, uint32_t height,
+                                float* color, float* depth, uint32_t* triangle_id, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
