@@ -199,6 +199,182 @@ def run_reference(args, world, rank):
     return 0
 
 
+class DeviceArray:
+    """A torch-visible view of a renderer-owned device buffer."""
+
+    def __init__(self, ptr, shape, typestr="<f4"):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
+def time_frames(r, stream, flush_l2, render, steps, warmup):
+    """Summed CUDA-event time (ms) of `steps` calls of render(), L2 flushed before each."""
+    import torch
+    for _ in range(warmup):
+        flush_l2()
+        render()
+    r.Synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for i in range(steps):
+        flush_l2()
+        starts[i].record(stream)
+        render()
+        ends[i].record(stream)
+    r.Synchronize()
+    torch.cuda.synchronize()
+    return sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+
+
+def measure_plain(sc, device, steps, warmup, flush_l2):
+    import torch
+    from edxraster_gb300 import renderer as R
+    stream = torch.cuda.Stream()
+    r = R.Renderer(device=device, stream=stream)
+    r.Initialize(sc.view.width, sc.view.height)
+    R.configure(r, sc.view)
+    dm = R.DeviceMesh.from_mesh(sc.mesh, device="cuda:%d" % device)
+    ms = time_frames(r, stream, lambda: flush_l2(stream), lambda: r.RenderMesh(dm, synchronize=False),
+                     steps, warmup) / steps
+    st = r.Stats()
+    r.close()
+    W, H = sc.view.width, sc.view.height
+    return {"triangles": sc.mesh.nt, "width": W, "height": H, "ms_per_frame": ms,
+            "mtris_per_s": sc.mesh.nt / ms / 1e3, "gpix_per_s": W * H / ms / 1e6, "fps": 1e3 / ms,
+            "hbm_frac": algorithmic_bytes(sc) / (ms / 1e3) / 1e9 / load_peaks()[0],
+            "raster_triangles": int(st.raster_triangles), "bin_entries": int(st.bin_entries)}
+
+
+def measure_batched(device, steps, warmup, flush_l2):
+    """256 meshes x 4 orbit views at 512x512: one batched pass vs one plain pass per view."""
+    import torch
+    from edxraster_gb300 import renderer as R
+    meshes = scenes.batched_meshes(256, 500, 200_000, seed=11)
+    views = []
+    for m in range(len(meshes)):
+        for v in scenes.orbit_views(4, 512, 512, seed=1000 + m):
+            v.mesh = m
+            views.append(v)
+    dms = [R.DeviceMesh.from_mesh(m, device="cuda:%d" % device) for m in meshes]
+    stream = torch.cuda.Stream()
+    r = R.Renderer(device=device, stream=stream)
+    r.Initialize(512, 512)
+    batch = r.PrepareBatch(dms, views)
+    ms_b = time_frames(r, stream, lambda: flush_l2(stream),
+                       lambda: r.RenderBatched(batch, None, 512, 512, synchronize=False), steps, warmup) / steps
+    sample = list(range(0, len(views), 97))
+    cb, db, tb = [], [], []
+    for i in sample:
+        c, d, t = r.ReadBatchOutputs(i, 1, 512, 512)
+        cb.append(c[0])
+        db.append(d[0])
+        tb.append(t[0])
+    # one plain pass per view, in submission order
+    p = R.Renderer(device=device, stream=stream)
+    p.Initialize(512, 512)
+
+    def per_view():
+        for v in views:
+            R.configure(p, v)
+            p.RenderMesh(dms[v.mesh], synchronize=False)
+
+    per_view()
+    p.Synchronize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    per_view()
+    p.Synchronize()
+    torch.cuda.synchronize()
+    ms_p = (time.perf_counter() - t0) * 1e3
+    exact = True
+    for j, i in enumerate(sample):
+        R.configure(p, views[i])
+        p.RenderMesh(dms[views[i].mesh])
+        c, d, t = p.ReadOutputs()
+        exact = exact and np.array_equal(t, tb[j]) and np.array_equal(d.view(np.uint32), db[j].view(np.uint32)) \
+            and np.array_equal(c, cb[j])
+    p.close()
+    r.close()
+    tris = sum(meshes[v.mesh].nt for v in views)
+    return {"views": len(views), "meshes": len(meshes), "triangles_per_pass": tris,
+            "batched_ms": ms_b, "views_per_s": len(views) / ms_b * 1e3,
+            "plain_one_pass_per_view_ms": ms_p, "plain_views_per_s": len(views) / ms_p * 1e3,
+            "speedup_vs_plain": ms_p / ms_b, "bit_exact_sampled_views": exact, "sampled_views": len(sample)}
+
+
+def measure_diff(device, steps, warmup):
+    """Torus of 50,000 triangles, 64 views at 256x256: forward vs forward + adjoint."""
+    import ctypes
+    import torch
+    from edxraster_gb300 import _lib
+    from edxraster_gb300 import renderer as R
+    mesh = scenes.diff_torus(seed=13)
+    views = scenes.orbit_views(64, 256, 256, seed=31)
+    rng = np.random.default_rng(17)
+    tgt = scenes.Mesh(mesh.positions * (1 + 0.05 * rng.uniform(-1, 1, size=mesh.positions.shape)).astype(np.float32),
+                      mesh.normals * (1 + 0.05 * rng.uniform(-1, 1, size=mesh.normals.shape)).astype(np.float32),
+                      np.clip(mesh.albedo * (1 + 0.05 * rng.uniform(-1, 1, size=mesh.albedo.shape)), 0, 1)
+                      .astype(np.float32), mesh.uvs, mesh.indices)
+    tviews = []
+    for v in views:
+        tv = scenes.View(**{k: getattr(v, k) for k in v.__dataclass_fields__})
+        tv.light = (v.light * (1 + 0.05 * rng.uniform(-1, 1, 3))).astype(np.float32)
+        tv.ks, tv.shininess = v.ks * 1.05, v.shininess * 1.05
+        tviews.append(tv)
+    stream = torch.cuda.Stream()
+    r = R.Renderer(device=device, stream=stream)
+    r.Initialize(256, 256)
+    dev = "cuda:%d" % device
+    r.RenderBatched([R.DeviceMesh.from_mesh(tgt, device=dev)], tviews, 256, 256)
+    o = r.BatchOutputs()
+    n = len(views)
+    target = torch.as_tensor(DeviceArray(o.color, (n, 256, 256, 4)), device=dev).clone()
+    dm = R.DeviceMesh.from_mesh(mesh, device=dev)
+    g_pos = torch.zeros_like(dm.positions)
+    g_nrm = torch.zeros_like(dm.normals)
+    g_alb = torch.zeros_like(dm.albedo)
+    g_glob = torch.zeros(5, device=dev)
+    grads = _lib.Grads(g_alb.data_ptr(), g_nrm.data_ptr(), g_pos.data_ptr(), g_glob.data_ptr(),
+                       g_glob.data_ptr() + 12, g_glob.data_ptr() + 16)
+    abi = dm.abi()
+    loss = torch.zeros((), device=dev)
+
+    def forward():
+        r.RenderBatched([dm], views, 256, 256, synchronize=False)
+        out = r.BatchOutputs()
+        c = torch.as_tensor(DeviceArray(out.color, (n, 256, 256, 4)), device=dev)
+        with torch.cuda.stream(stream):
+            loss.copy_(((c - target) ** 2).sum())
+        return c
+
+    def forward_backward():
+        c = forward()
+        with torch.cuda.stream(stream):
+            grad = 2.0 * (c - target)
+            for t in (g_pos, g_nrm, g_alb, g_glob):
+                t.zero_()
+        _lib.check(r._lib.edxr_backward(r._h, ctypes.byref(abi), None, grad.data_ptr(), ctypes.byref(grads)))
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    ms_f = timed(forward)
+    ms_fb = timed(forward_backward)
+    r.close()
+    return {"triangles": mesh.nt, "views": n, "width": 256, "height": 256, "fwd_ms": ms_f,
+            "fwd_iters_per_s": 1e3 / ms_f, "fwd_bwd_ms": ms_fb, "fwd_bwd_iters_per_s": 1e3 / ms_fb,
+            "fwd_bwd_over_fwd": ms_fb / ms_f}
+
+
 def run_gpu(args, world, rank, local):
     import torch
     from edxraster_gb300 import renderer as R
@@ -290,6 +466,18 @@ def run_gpu(args, world, rank, local):
     e2e_value = world * sc.mesh.nt * args.steps / e2e_s / 1e6
     r.close()
 
+    # ---- the other configurations (same GPU, shorter runs) ----------------
+    per_config = {}
+    if not args.no_configs and rank == 0:
+        def flush_on(s):
+            with torch.cuda.stream(s):
+                flush.zero_()
+        for wname in ("sphere", "stress"):
+            if wname != args.workload:
+                per_config[wname] = measure_plain(WORKLOADS[wname][1](), local, max(3, args.steps // 4), 3, flush_on)
+        per_config["batched"] = measure_batched(local, 3, 3, flush_on)
+        per_config["differentiable"] = measure_diff(local, 5, 3)
+
     if rank != 0:
         return 0
     cpu = None
@@ -317,6 +505,7 @@ def run_gpu(args, world, rank, local):
         "clocks": clock_info,
         "raster_triangles": int(stats.raster_triangles), "bin_entries": int(stats.bin_entries),
         "cpu_baseline": cpu,
+        "per_config": per_config,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -332,6 +521,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="terrain", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the per-configuration measurements")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

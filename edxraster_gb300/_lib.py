@@ -95,8 +95,10 @@ SIGNATURES = {
     "edxr_render_batched": ([_P, ctypes.POINTER(Mesh), ctypes.c_uint32, ctypes.POINTER(View), ctypes.c_uint32,
                              ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
     "edxr_get_batch_outputs": ([_P, ctypes.POINTER(BatchOutputs)], ctypes.c_int),
-    "edxr_shade_visible": ([_P, ctypes.POINTER(Mesh), _P], ctypes.c_int),
-    "edxr_backward": ([_P, ctypes.POINTER(Mesh), _P, ctypes.POINTER(Grads)], ctypes.c_int),
+    "edxr_read_batch_outputs": ([_P, ctypes.c_uint32, ctypes.c_uint32, _P, _P, _P], ctypes.c_int),
+    "edxr_shade_visible": ([_P, ctypes.POINTER(Mesh), ctypes.POINTER(ShaderParams), _P], ctypes.c_int),
+    "edxr_backward": ([_P, ctypes.POINTER(Mesh), ctypes.POINTER(ShaderParams), _P, ctypes.POINTER(Grads)],
+                      ctypes.c_int),
     "edxr_render_noalloc": ([ctypes.POINTER(Mesh), _P, _P, _P, ctypes.POINTER(State), ctypes.c_int,
                              ctypes.POINTER(ShaderParams), ctypes.c_uint32, ctypes.c_uint32, _P, _P, _P, _P],
                             ctypes.c_int),

@@ -147,7 +147,7 @@ struct edxr_renderer
     Camera cam;
 
     DevBuf frames, clip, rtris, polys, tile_count, tile_offset, tile_cursor, bins, big_list, counters, status;
-    DevBuf color, depth, tri_id, back8;
+    DevBuf color, depth, tri_id, back8, diff_scratch;
     uint64_t bin_capacity = 0, rtri_cap = 0, poly_cap = 0, big_cap = 0;
     std::vector<MeshStage> stage;
     FrameDesc* frames_host = nullptr;  // pinned
@@ -166,6 +166,8 @@ struct edxr_renderer
     bool use_graphs = true;
     cudaGraphExec_t graph = nullptr;
     PassArgs graph_args = {};
+    PassArgs prev_args = {};
+    bool has_prev_args = false;
 
     // stage timing
     bool profiling = false;
@@ -184,6 +186,13 @@ cudaError_t run_pass(edxr_renderer* r, const PassArgs& a)
         return launch_pipeline(a, r->stream);
     if (r->graph && same_args(a, r->graph_args))
         return cudaGraphLaunch(r->graph, r->stream);
+    // Capture only once the same pass layout repeats: a caller that changes
+    // meshes every frame gets direct launches instead of a capture per frame.
+    const bool repeat = r->has_prev_args && same_args(a, r->prev_args);
+    r->prev_args = a;
+    r->has_prev_args = true;
+    if (!repeat)
+        return launch_pipeline(a, r->stream);
     if (r->graph)
     {
         cudaGraphExecDestroy(r->graph);
@@ -555,7 +564,7 @@ edxr_status edxr_destroy(edxr_renderer* r)
         cudaGraphExecDestroy(r->graph);
     DevBuf* bufs[] = { &r->frames, &r->clip, &r->rtris, &r->polys, &r->tile_count, &r->tile_offset,
                        &r->tile_cursor, &r->bins, &r->big_list, &r->counters, &r->status, &r->color,
-                       &r->depth, &r->tri_id, &r->back8 };
+                       &r->depth, &r->tri_id, &r->back8, &r->diff_scratch };
     for (DevBuf* b : bufs)
         b->release();
     for (auto& s : r->stage)
@@ -836,20 +845,106 @@ edxr_status edxr_get_batch_outputs(edxr_renderer* r, edxr_batch_outputs* out)
     return EDXR_OK;
 }
 
-edxr_status edxr_shade_visible(edxr_renderer* r, const edxr_mesh* mesh, float* color_out)
+edxr_status edxr_read_batch_outputs(edxr_renderer* r, uint32_t first_view, uint32_t num_views, float* color,
+                                    float* depth, uint32_t* id)
 {
-    (void)mesh; (void)color_out;
     if (!r)
         return fail(EDXR_ERR_INVALID_ARG, "NULL renderer");
-    return fail(EDXR_ERR_UNSUPPORTED, "edxr_shade_visible is not built yet");
+    DeviceGuard g(r->device);
+    edxr_status s = sync_pass(r);
+    if (s != EDXR_OK)
+        return s;
+    if (!r->last_frames || (uint64_t)first_view + num_views > r->last_frames)
+        return fail(EDXR_ERR_INVALID_ARG, "view range outside the last pass");
+    const size_t per = (size_t)r->out_width * r->out_height;
+    const size_t off = per * first_view, n = per * num_views;
+    if (color) EDXR_CUDA(cudaMemcpyAsync(color, r->color.as<float>() + 4 * off, 16 * n, cudaMemcpyDeviceToHost, r->stream));
+    if (depth) EDXR_CUDA(cudaMemcpyAsync(depth, r->depth.as<float>() + off, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    if (id) EDXR_CUDA(cudaMemcpyAsync(id, r->tri_id.as<uint32_t>() + off, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    EDXR_CUDA(cudaStreamSynchronize(r->stream));
+    return EDXR_OK;
 }
 
-edxr_status edxr_backward(edxr_renderer* r, const edxr_mesh* mesh, const float* grad_color, const edxr_grads* grads)
+namespace {
+
+// The mesh of the differentiable form must be device-resident and have the
+// vertex/triangle counts every frame of the last pass was rendered with.
+edxr_status diff_mesh(edxr_renderer* r, const edxr_mesh* mesh, const edxr_shader_params* params, DiffMesh* m)
 {
-    (void)mesh; (void)grad_color; (void)grads;
-    if (!r)
-        return fail(EDXR_ERR_INVALID_ARG, "NULL renderer");
-    return fail(EDXR_ERR_UNSUPPORTED, "edxr_backward is not built yet");
+    edxr_status s = check_mesh(mesh);
+    if (s != EDXR_OK)
+        return s;
+    std::memset(m, 0, sizeof(*m));
+    if (params)
+    {
+        m->override_shading = 1;
+        for (int q = 0; q < 3; q++)
+            m->light[q] = params->light[q];
+        m->ks = params->ks;
+        m->shininess = params->shininess;
+    }
+    if (mesh->memory != EDXR_MEMORY_DEVICE)
+        return fail(EDXR_ERR_INVALID_ARG, "the differentiable form takes a device-memory mesh");
+    if ((s = sync_pass(r)) != EDXR_OK)
+        return s;
+    if (!r->last_frames)
+        return fail(EDXR_ERR_INVALID_ARG, "nothing rendered yet");
+    for (uint32_t i = 0; i < r->last_frames; i++)
+        if (r->frames_host[i].nv != mesh->num_vertices || r->frames_host[i].nt != mesh->num_triangles)
+            return fail(EDXR_ERR_INVALID_ARG, "mesh sizes differ from the mesh of the last pass");
+    m->positions = static_cast<const char*>(mesh->positions);
+    m->normals = static_cast<const char*>(mesh->normals);
+    m->albedo = static_cast<const char*>(mesh->albedo);
+    m->indices = mesh->indices;
+    m->pos_stride = mesh->position_stride;
+    m->nrm_stride = mesh->normal_stride;
+    m->alb_stride = mesh->albedo_stride;
+    m->nv = mesh->num_vertices;
+    m->nt = mesh->num_triangles;
+    return EDXR_OK;
+}
+
+}  // namespace
+
+edxr_status edxr_shade_visible(edxr_renderer* r, const edxr_mesh* mesh, const edxr_shader_params* params,
+                               float* color_out)
+{
+    if (!r || !color_out)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    DeviceGuard g(r->device);
+    DiffMesh m;
+    edxr_status s = diff_mesh(r, mesh, params, &m);
+    if (s != EDXR_OK)
+        return s;
+    const uint64_t total = (uint64_t)r->last_frames * r->out_width * r->out_height;
+    EDXR_CUDA(launch_shade_visible(r->last, total, m, reinterpret_cast<float4*>(color_out), r->stream));
+    EDXR_CUDA(cudaStreamSynchronize(r->stream));
+    return EDXR_OK;
+}
+
+edxr_status edxr_backward(edxr_renderer* r, const edxr_mesh* mesh, const edxr_shader_params* params,
+                          const float* grad_color, const edxr_grads* grads)
+{
+    if (!r || !grad_color || !grads)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    DeviceGuard g(r->device);
+    DiffMesh m;
+    edxr_status s = diff_mesh(r, mesh, params, &m);
+    if (s != EDXR_OK)
+        return s;
+    EDXR_CUDA(r->diff_scratch.ensure(8 * sizeof(double)));
+    DiffGrads dg;
+    dg.albedo = grads->albedo;
+    dg.normals = grads->normals;
+    dg.positions = grads->positions;
+    dg.light = grads->light;
+    dg.ks = grads->ks;
+    dg.shininess = grads->shininess;
+    dg.scratch = r->diff_scratch.as<double>();
+    const uint64_t total = (uint64_t)r->last_frames * r->out_width * r->out_height;
+    EDXR_CUDA(launch_backward(r->last, total, m, reinterpret_cast<const float4*>(grad_color), dg, r->stream));
+    EDXR_CUDA(cudaEventRecord(r->done, r->stream));
+    return EDXR_OK;
 }
 
 }  // extern "C"

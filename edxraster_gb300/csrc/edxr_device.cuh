@@ -152,7 +152,7 @@ __device__ __forceinline__ PolyVert plane_cut(int plane, const PolyVert& a, cons
 // Clipper::ClipPolygon (Clipper.h:235-288): Sutherland-Hodgman against the
 // planes in planeCode, in the order L, R, B, T, F, N, then the polygon is
 // dropped when any vertex has w <= 0.  Returns the vertex count.
-__device__ __noinline__ int clip_polygon(PolyVert* poly, uint32_t planeCode)
+static __device__ __noinline__ int clip_polygon(PolyVert* poly, uint32_t planeCode)
 {
     PolyVert tmp[kMaxPolygon];
     int n = 3;
@@ -501,7 +501,7 @@ __device__ __forceinline__ float3 shade_model(const FrameDesc& f, float3 P, floa
 // the error of N.H by ks*s*x^(s-1) = 600: FP32 unit vectors cannot hold N.H
 // to the ~5e-9 that 1e-5 of colour needs, so this shader interpolates and
 // shades in FP64.
-__device__ __noinline__ float3 shade_fragment_fp64(const FrameDesc& f, const RTri& t, const ClipPoly* polys,
+static __device__ __noinline__ float3 shade_fragment_fp64(const FrameDesc& f, const RTri& t, const ClipPoly* polys,
                                                    float l0, float l1)
 {
     double b0 = l0, b1 = l1;

@@ -126,8 +126,25 @@ int kernels_per_pass(const PassArgs& a);
 void record_error(const char* msg);
 void prepare_kernels();
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s);
-cudaError_t launch_shade_visible(const PassArgs& a, float4* out, cudaStream_t s);
-cudaError_t launch_backward(const PassArgs& a, const float4* grad, float* g_alb, float* g_nrm, float* g_pos,
-                            float* g_light, float* g_ks, float* g_shin, cudaStream_t s);
+// Mesh used by the differentiable form (device pointers, strides in bytes).
+struct DiffMesh
+{
+    const char* positions; const char* normals; const char* albedo;
+    const uint32_t* indices;
+    uint32_t pos_stride, nrm_stride, alb_stride;
+    uint32_t nv, nt;
+    int override_shading;   // 1: use light/ks/shininess below for every frame
+    float light[3], ks, shininess;
+};
+struct DiffGrads
+{
+    float* albedo; float* normals; float* positions;  // nv*3 each, may be NULL
+    float* light; float* ks; float* shininess;         // may be NULL
+    double* scratch;                                    // 5 doubles, zeroed by the launcher
+};
+cudaError_t launch_shade_visible(const PassArgs& a, uint64_t total_pixels, const DiffMesh& m, float4* out,
+                                 cudaStream_t s);
+cudaError_t launch_backward(const PassArgs& a, uint64_t total_pixels, const DiffMesh& m, const float4* grad,
+                            const DiffGrads& g, cudaStream_t s);
 
 }  // namespace edxr

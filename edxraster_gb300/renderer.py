@@ -262,8 +262,9 @@ class Renderer:
         return {self.STAGES[i]: float(ms[i]) for i in range(n.value)}
 
     # -- batched form ----------------------------------------------------------
-    def RenderBatched(self, meshes, views, width: int, height: int, synchronize: bool = True):
-        """Render every (mesh, view) pair in one pass; views are scenes.View with a .mesh index."""
+    @staticmethod
+    def PrepareBatch(meshes, views):
+        """ABI arrays for a batched pass, built once and reusable across calls."""
         keeps, abis = [], []
         for m in meshes:
             k, a = _as_abi_mesh(m)
@@ -279,8 +280,15 @@ class Renderer:
             varr[i].shading = _lib.ShaderParams((ctypes.c_float * 3)(*[float(x) for x in v.light]), v.ks, v.shininess)
             varr[i].ps_kind = v.shader
             varr[i].depth_func = v.depth_func
-        self._keep = (keeps, marr, varr)
-        _lib.check(self._lib.edxr_render_batched(self._h, marr, len(abis), varr, len(views), width, height))
+        return (keeps, marr, len(abis), varr, len(views))
+
+    def RenderBatched(self, meshes, views, width: int, height: int, synchronize: bool = True):
+        """Render every (mesh, view) pair in one pass; views are scenes.View with a .mesh index.
+        `meshes` may instead be the result of PrepareBatch (then `views` is ignored)."""
+        batch = meshes if isinstance(meshes, tuple) else self.PrepareBatch(meshes, views)
+        self._keep = batch
+        _, marr, nm, varr, nv = batch
+        _lib.check(self._lib.edxr_render_batched(self._h, marr, nm, varr, nv, width, height))
         if synchronize:
             self.Synchronize()
 
@@ -288,6 +296,14 @@ class Renderer:
         o = _lib.BatchOutputs()
         _lib.check(self._lib.edxr_get_batch_outputs(self._h, ctypes.byref(o)))
         return o
+
+    def ReadBatchOutputs(self, first: int, count: int, width: int, height: int):
+        color = np.empty((count, height, width, 4), np.float32)
+        depth = np.empty((count, height, width), np.float32)
+        tid = np.empty((count, height, width), np.uint32)
+        _lib.check(self._lib.edxr_read_batch_outputs(self._h, first, count, color.ctypes.data, depth.ctypes.data,
+                                                     tid.ctypes.data))
+        return color, depth, tid
 
 
 def configure(r: Renderer, view, hierarchical: bool = True):

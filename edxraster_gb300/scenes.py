@@ -40,6 +40,7 @@ class View:
     shininess: float = 32.0
     shader: int = SHADER_BLINN_PHONG
     depth_func: int = DEPTH_LESS
+    mesh: int = 0        # mesh index, for batched rendering
 
 
 @dataclasses.dataclass
@@ -142,35 +143,27 @@ def uv_sphere(slices: int, stacks: int, radius: float = 1.0, center=(0, 0, 0)) -
     Triangles: 2*slices*(stacks-1); vertices: slices*(stacks-1) + 2.
     """
     center = np.asarray(center, np.float64)
-    rings = []
-    uvs = []
-    rings.append([0.0, 1.0, 0.0]); uvs.append([0.5, 0.0])
-    for j in range(1, stacks):
-        th = math.pi * j / stacks
-        for i in range(slices):
-            ph = 2.0 * math.pi * i / slices
-            rings.append([math.sin(th) * math.cos(ph), math.cos(th), math.sin(th) * math.sin(ph)])
-            uvs.append([i / slices, j / stacks])
-    rings.append([0.0, -1.0, 0.0]); uvs.append([0.5, 1.0])
-    nrm = np.asarray(rings, np.float64)
+    J, I = np.meshgrid(np.arange(1, stacks), np.arange(slices), indexing="ij")
+    th = np.pi * J / stacks
+    ph = 2.0 * np.pi * I / slices
+    ring_n = np.stack([np.sin(th) * np.cos(ph), np.cos(th), np.sin(th) * np.sin(ph)], -1).reshape(-1, 3)
+    ring_uv = np.stack([I / slices, J / stacks], -1).reshape(-1, 2)
+    nrm = np.concatenate([[[0.0, 1.0, 0.0]], ring_n, [[0.0, -1.0, 0.0]]], 0)
+    uvs = np.concatenate([[[0.5, 0.0]], ring_uv, [[0.5, 1.0]]], 0)
     pos = center + radius * nrm
-    north, south = 0, len(rings) - 1
+    north, south = 0, len(nrm) - 1
 
     def ring(j, i):
         return 1 + (j - 1) * slices + (i % slices)
 
-    tris = []
-    for i in range(slices):
-        tris.append([north, ring(1, i), ring(1, i + 1)])
-    for j in range(1, stacks - 1):
-        for i in range(slices):
-            a, b = ring(j, i), ring(j, i + 1)
-            c, d = ring(j + 1, i), ring(j + 1, i + 1)
-            tris.append([a, c, b])
-            tris.append([b, c, d])
-    for i in range(slices):
-        tris.append([south, ring(stacks - 1, i + 1), ring(stacks - 1, i)])
-    idx = np.asarray(tris, np.int64)
+    i = np.arange(slices)
+    cap_n = np.stack([np.full(slices, north), ring(1, i), ring(1, i + 1)], -1)
+    jj, ii = np.meshgrid(np.arange(1, stacks - 1), np.arange(slices), indexing="ij")
+    a, b = ring(jj, ii), ring(jj, ii + 1)
+    c, d = ring(jj + 1, ii), ring(jj + 1, ii + 1)
+    band = np.stack([np.stack([a, c, b], -1), np.stack([b, c, d], -1)], 2).reshape(-1, 3)
+    cap_s = np.stack([np.full(slices, south), ring(stacks - 1, i + 1), ring(stacks - 1, i)], -1)
+    idx = np.concatenate([cap_n, band, cap_s], 0).astype(np.int64)
     cent = pos[idx].mean(axis=1) - center
     idx = _orient_outward(pos, idx, cent).astype(np.uint32)
     return Mesh(pos.astype(np.float32), nrm.astype(np.float32),

@@ -228,6 +228,11 @@ edxr_status edxr_render_batched(edxr_renderer* r, const edxr_mesh* meshes, uint3
 
 edxr_status edxr_get_batch_outputs(edxr_renderer* r, edxr_batch_outputs* out);
 
+/* Copy views [first_view, first_view + num_views) of the last batched pass
+ * to host memory; any pointer may be NULL (synchronizes). */
+edxr_status edxr_read_batch_outputs(edxr_renderer* r, uint32_t first_view, uint32_t num_views, float* color,
+                                    float* depth, uint32_t* triangle_id);
+
 /* ---- differentiable form -------------------------------------------------- */
 
 /* Gradient outputs, device memory; NULL members are skipped.  The adjoint
@@ -242,19 +247,24 @@ typedef struct edxr_grads
     float* shininess;  /* 1 */
 } edxr_grads;
 
-/* Shade the visible surface of the last edxr_render again, with visibility
- * (the triangle-id buffer) held fixed and perspective-correct barycentrics
- * taken from the un-snapped clip-space vertices, writing RGBA32F into
- * color_out (device, width*height*4).  This is the forward function whose
- * gradient edxr_backward computes. */
-edxr_status edxr_shade_visible(edxr_renderer* r, const edxr_mesh* mesh, float* color_out);
+/* Shade the visible surface of the last pass (edxr_render or
+ * edxr_render_batched) again, with visibility (the triangle-id buffer) held
+ * fixed and perspective-correct barycentrics taken from the un-snapped
+ * clip-space vertices of `mesh` (device memory, same sizes as the rendered
+ * mesh), writing RGBA32F into color_out (device, frames*height*width*4).
+ * Cameras come from the pass; light, ks and shininess from `params`, or from
+ * each frame when params is NULL.  This is the forward function whose
+ * gradient edxr_backward computes (synchronizes). */
+edxr_status edxr_shade_visible(edxr_renderer* r, const edxr_mesh* mesh, const edxr_shader_params* params,
+                               float* color_out);
 
-/* Adjoint of edxr_shade_visible: given dL/dcolor (device, width*height*4,
+/* Adjoint of edxr_shade_visible: given dL/dcolor (device, same layout,
  * alpha ignored) accumulate dL/d{albedo, normals, positions, light, ks,
  * shininess}.  Recomputes everything per pixel from the triangle-id buffer;
- * no per-pixel intermediates are stored by the forward pass. */
-edxr_status edxr_backward(edxr_renderer* r, const edxr_mesh* mesh, const float* grad_color,
-                          const edxr_grads* grads);
+ * no per-pixel intermediates are stored by the forward pass.  Asynchronous
+ * on the renderer's stream. */
+edxr_status edxr_backward(edxr_renderer* r, const edxr_mesh* mesh, const edxr_shader_params* params,
+                          const float* grad_color, const edxr_grads* grads);
 
 /* ---- rendering without device allocation ---------------------------------- */
 
