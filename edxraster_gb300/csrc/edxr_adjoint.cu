@@ -85,27 +85,48 @@ __device__ __forceinline__ bool pixel_forward(const FrameDesc& f, const DiffMesh
         s.p[k] = ld(m.positions, m.pos_stride, s.vi[k], 0.0f);
         s.n[k] = ld(m.normals, m.nrm_stride, s.vi[k], 0.0f);
         s.a[k] = ld(m.albedo, m.alb_stride, s.vi[k], 1.0f);
-        const float4 c = xform_point4(f.mvp, s.p[k].x, s.p[k].y, s.p[k].z);
-        s.X[k] = c.x;
-        s.Y[k] = c.y;
-        s.W[k] = c.w;
     }
-    const float rx = (float)px + 0.5f, ry = (float)py + 0.5f;
-    s.u = f.ndc_from_raster[0] * rx + f.ndc_from_raster[1] * ry + f.ndc_from_raster[2];
-    s.v = f.ndc_from_raster[3] * rx + f.ndc_from_raster[4] * ry + f.ndc_from_raster[5];
+    // The solve cancels heavily (a_k, c_k are the small projected distances of
+    // the vertices from the pixel centre, each a difference of O(1) terms), so
+    // the clip coordinates, the pixel centre and the solve run in FP64; the
+    // result is rounded to float once.
+    double X[3], Y[3], Wd[3], ac[3], cc[3], bt[3];
+    const float* M = f.mvp;
     for (int k = 0; k < 3; k++)
     {
-        s.ac[k] = s.X[k] - s.u * s.W[k];
-        s.cc[k] = s.Y[k] - s.v * s.W[k];
+        const double x = s.p[k].x, y = s.p[k].y, z = s.p[k].z;
+        X[k] = (double)M[0] * x + (double)M[1] * y + (double)M[2] * z + (double)M[3];
+        Y[k] = (double)M[4] * x + (double)M[5] * y + (double)M[6] * z + (double)M[7];
+        Wd[k] = (double)M[12] * x + (double)M[13] * y + (double)M[14] * z + (double)M[15];
+        s.X[k] = (float)X[k];
+        s.Y[k] = (float)Y[k];
+        s.W[k] = (float)Wd[k];
     }
-    s.bt[0] = s.ac[1] * s.cc[2] - s.ac[2] * s.cc[1];
-    s.bt[1] = s.ac[2] * s.cc[0] - s.ac[0] * s.cc[2];
-    s.bt[2] = s.ac[0] * s.cc[1] - s.ac[1] * s.cc[0];
-    s.S = s.bt[0] + s.bt[1] + s.bt[2];
-    if (!(s.S != 0.0f))
-        return false;
+    const double rx = (double)px + 0.5, ry = (double)py + 0.5;
+    const double* R = f.ndc_from_raster_d;
+    const double u = R[0] * rx + R[1] * ry + R[2];
+    const double v = R[3] * rx + R[4] * ry + R[5];
+    s.u = (float)u;
+    s.v = (float)v;
     for (int k = 0; k < 3; k++)
-        s.b[k] = s.bt[k] / s.S;
+    {
+        ac[k] = X[k] - u * Wd[k];
+        cc[k] = Y[k] - v * Wd[k];
+        s.ac[k] = (float)ac[k];
+        s.cc[k] = (float)cc[k];
+    }
+    bt[0] = ac[1] * cc[2] - ac[2] * cc[1];
+    bt[1] = ac[2] * cc[0] - ac[0] * cc[2];
+    bt[2] = ac[0] * cc[1] - ac[1] * cc[0];
+    const double S = bt[0] + bt[1] + bt[2];
+    if (!(S != 0.0))
+        return false;
+    s.S = (float)S;
+    for (int k = 0; k < 3; k++)
+    {
+        s.bt[k] = (float)bt[k];
+        s.b[k] = (float)(bt[k] / S);
+    }
     s.P = s.b[0] * s.p[0] + s.b[1] * s.p[1] + s.b[2] * s.p[2];
     s.Nraw = s.b[0] * s.n[0] + s.b[1] * s.n[1] + s.b[2] * s.n[2];
     s.A = s.b[0] * s.a[0] + s.b[1] * s.a[1] + s.b[2] * s.a[2];

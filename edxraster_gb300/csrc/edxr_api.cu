@@ -324,12 +324,14 @@ void fill_frame(FrameDesc& f, const edxr_mesh& m, const Camera& cam, const Shadi
     const double det = a * e - b * d;
     if (det != 0.0)
     {
-        f.ndc_from_raster[0] = (float)(e / det);
-        f.ndc_from_raster[1] = (float)(-b / det);
-        f.ndc_from_raster[2] = (float)((b * g - e * c) / det);
-        f.ndc_from_raster[3] = (float)(-d / det);
-        f.ndc_from_raster[4] = (float)(a / det);
-        f.ndc_from_raster[5] = (float)((d * c - a * g) / det);
+        f.ndc_from_raster_d[0] = e / det;
+        f.ndc_from_raster_d[1] = -b / det;
+        f.ndc_from_raster_d[2] = (b * g - e * c) / det;
+        f.ndc_from_raster_d[3] = -d / det;
+        f.ndc_from_raster_d[4] = a / det;
+        f.ndc_from_raster_d[5] = (d * c - a * g) / det;
+        for (int q = 0; q < 6; q++)
+            f.ndc_from_raster[q] = (float)f.ndc_from_raster_d[q];
     }
 }
 

@@ -52,6 +52,7 @@ struct FrameDesc
     float light_raw[3];        // light direction as given (FP64 shading normalises it)
     float pad2;
     double eye_d[3];           // eye position in double (FP64 shading)
+    double ndc_from_raster_d[6];  // the raster-to-NDC inverse in double (differentiable form)
 };
 
 // One triangle after clipping and setup (RasterTriangle, RasterTriangle.h:11-24),

@@ -26,6 +26,22 @@ def _ndc_from_raster(raster):
     return Ai, -Ai @ t
 
 
+def mvp_float32(proj, mv):
+    """P * MV as the pipeline forms it (Renderer.cpp:90): float32, each entry
+    summed left to right.  The differentiable forward takes this float matrix
+    as the given transform."""
+    P = np.asarray(proj, np.float32).reshape(4, 4)
+    M = np.asarray(mv, np.float32).reshape(4, 4)
+    C = np.zeros((4, 4), np.float32)
+    for i in range(4):
+        for j in range(4):
+            s = np.float32(P[i, 0] * M[0, j])
+            for k in range(1, 4):
+                s = np.float32(s + np.float32(P[i, k] * M[k, j]))
+            C[i, j] = s
+    return C
+
+
 def _eye(mv):
     inv = np.linalg.inv(np.asarray(mv, np.float64).reshape(4, 4))
     return inv[:3, 3] / inv[3, 3]
@@ -47,8 +63,7 @@ def shade_visible(positions, normals, albedo, indices, light, ks, shininess, vie
         p = positions[vi]                              # (n,3,3)
         n = normals[vi]
         a = albedo[vi]
-        mvp = torch.as_tensor(np.asarray(view.proj, np.float64).reshape(4, 4) @
-                              np.asarray(view.mv, np.float64).reshape(4, 4))
+        mvp = torch.as_tensor(mvp_float32(view.proj, view.mv).astype(np.float64))
         ph = torch.cat([p, torch.ones_like(p[..., :1])], -1)
         clip = ph @ mvp.T                              # (n,3,4)
         X, Y, Wc = clip[..., 0], clip[..., 1], clip[..., 3]

@@ -31,7 +31,8 @@ def setup(nviews=4, size=96, shader=0):
     dm = R.DeviceMesh.from_mesh(mesh)
     r.RenderBatched([dm], views, size, size)
     _, _, ids = r.ReadBatchOutputs(0, nviews, size, size)
-    grad = torch.randn((nviews, size, size, 4), dtype=torch.float32, device="cuda", generator=None)
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    grad = torch.randn((nviews, size, size, 4), dtype=torch.float32, device="cuda", generator=gen)
     return mesh, views, light, r, dm, ids, grad
 
 
