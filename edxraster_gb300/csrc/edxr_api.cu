@@ -146,9 +146,10 @@ struct edxr_renderer
     Shading shading;
     Camera cam;
 
-    DevBuf frames, clip, rtris, polys, tile_count, tile_offset, tile_cursor, bins, big_list, counters, status;
+    DevBuf frames, clip, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, bins, big_list, counters, status;
     DevBuf color, depth, tri_id, back8, diff_scratch;
     uint64_t bin_capacity = 0, rtri_cap = 0, poly_cap = 0, big_cap = 0;
+    uint64_t debug_cap = 0;  // EDXR_DEBUG_CAPACITY: tiny starting capacities (tests)
     std::vector<MeshStage> stage;
     FrameDesc* frames_host = nullptr;  // pinned
     size_t frames_host_cap = 0;
@@ -354,19 +355,28 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
         return fail(EDXR_ERR_OVERFLOW, "pass too large: reduce the number of frames per call");
     const uint64_t pixels = (uint64_t)n * width * height;
     // Intermediate capacities start from typical needs and grow when a frame
-    // reports an overflow (sync_pass renders that frame again).
-    r->rtri_cap = std::max<uint64_t>({ r->rtri_cap, tt + std::max<uint64_t>(tt / 4, 65536) });
-    r->poly_cap = std::max<uint64_t>({ r->poly_cap, std::max<uint64_t>(tt / 16, 65536) });
-    r->big_cap = std::max<uint64_t>({ r->big_cap, std::max<uint64_t>(tt / 8, 65536) });
+    // reports an overflow (sync_pass renders that frame again).  The test
+    // knob EDXR_DEBUG_CAPACITY starts them all tiny instead, so the first
+    // frame exercises that recovery.
+    if (r->debug_cap && r->rtri_cap == 0)
+        r->rtri_cap = r->poly_cap = r->big_cap = r->bin_capacity = r->debug_cap;
+    else
+        r->rtri_cap = std::max<uint64_t>({ r->rtri_cap, tt + std::max<uint64_t>(tt / 4, 65536) });
+    if (!r->debug_cap)
+    {
+        r->poly_cap = std::max<uint64_t>({ r->poly_cap, std::max<uint64_t>(tt / 16, 65536) });
+        r->big_cap = std::max<uint64_t>({ r->big_cap, std::max<uint64_t>(tt / 8, 65536) });
+        if (r->bin_capacity < 2 * tt + 4 * tiles)
+            r->bin_capacity = std::max<uint64_t>(2 * tt + 4 * tiles, 1u << 20);
+    }
     r->rtri_cap = std::min<uint64_t>(r->rtri_cap, 0xFFFFFFF0u);
     const uint64_t rcap = r->rtri_cap, pcap = r->poly_cap;
     const uint64_t nscan = (tiles + 4095) / 4096;
-    if (r->bin_capacity < 2 * tt + 4 * tiles)
-        r->bin_capacity = std::max<uint64_t>(2 * tt + 4 * tiles, 1u << 20);
     EDXR_CUDA(r->frames.ensure(sizeof(FrameDesc) * n));
     EDXR_CUDA(r->clip.ensure(sizeof(float4) * std::max<uint64_t>(tv, 1)));
     EDXR_CUDA(r->rtris.ensure(sizeof(RTri) * rcap));
     EDXR_CUDA(r->polys.ensure(sizeof(ClipPoly) * pcap));
+    EDXR_CUDA(r->clip_list.ensure(4 * pcap));
     EDXR_CUDA(r->tile_count.ensure(4 * (tiles + 1)));
     EDXR_CUDA(r->tile_offset.ensure(4 * (tiles + 1)));
     EDXR_CUDA(r->tile_cursor.ensure(4 * (tiles + 1 + nscan + 1)));
@@ -391,6 +401,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.rtris = r->rtris.as<RTri>();
     a.rtri_capacity = (uint32_t)std::min<uint64_t>(rcap, 0xFFFFFFFFu);
     a.polys = r->polys.as<ClipPoly>();
+    a.clip_list = r->clip_list.as<uint32_t>();
     a.poly_capacity = (uint32_t)pcap;
     a.tile_count = r->tile_count.as<uint32_t>();
     a.tile_offset = r->tile_offset.as<uint32_t>();
@@ -469,7 +480,9 @@ edxr_status sync_pass(edxr_renderer* r)
         {
             r->poly_cap = (uint64_t)st.clipped_polys + st.clipped_polys / 4 + 1024;
             EDXR_CUDA(r->polys.ensure(sizeof(ClipPoly) * r->poly_cap));
+            EDXR_CUDA(r->clip_list.ensure(4 * r->poly_cap));
             a.polys = r->polys.as<ClipPoly>();
+            a.clip_list = r->clip_list.as<uint32_t>();
             a.poly_capacity = (uint32_t)r->poly_cap;
         }
         if (st.overflow & 8u)
@@ -542,6 +555,8 @@ edxr_status edxr_create(edxr_renderer** out, const edxr_init* init)
     prepare_kernels();  // occupancy queries happen outside any graph capture
     if (const char* e = std::getenv("EDXR_NO_GRAPHS"))
         r->use_graphs = e[0] == '0';
+    if (const char* e = std::getenv("EDXR_DEBUG_CAPACITY"))
+        r->debug_cap = std::max<uint64_t>(std::strtoull(e, nullptr, 10), 4);
     cudaError_t e = cudaMallocHost((void**)&r->status_host, sizeof(DeviceStatus));
     if (e == cudaSuccess)
         e = cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming);
@@ -564,7 +579,7 @@ edxr_status edxr_destroy(edxr_renderer* r)
         cudaEventSynchronize(r->done);
     if (r->graph)
         cudaGraphExecDestroy(r->graph);
-    DevBuf* bufs[] = { &r->frames, &r->clip, &r->rtris, &r->polys, &r->tile_count, &r->tile_offset,
+    DevBuf* bufs[] = { &r->frames, &r->clip, &r->rtris, &r->polys, &r->clip_list, &r->tile_count, &r->tile_offset,
                        &r->tile_cursor, &r->bins, &r->big_list, &r->counters, &r->status, &r->color,
                        &r->depth, &r->tri_id, &r->back8, &r->diff_scratch };
     for (DevBuf* b : bufs)

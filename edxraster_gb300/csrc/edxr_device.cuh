@@ -64,15 +64,19 @@ __device__ __forceinline__ void xform_point3(const float* M, float x, float y, f
     }
 }
 
-// v.x = a.x * 16.0 (RasterTriangle.h:35-40): the product is taken in double and
-// truncated toward zero; NaN and out-of-range give INT_MIN, as the x86
-// cvttsd2si conversion of the reference does.
+// v.x = a.x * 16.0 (RasterTriangle.h:35-40): the reference multiplies in
+// double and truncates toward zero; NaN and out-of-range give INT_MIN, as the
+// x86 cvttsd2si conversion does.  Scaling by 16 is exact in float as well
+// (no float reaches overflow by it, and subnormals scale exactly), so the
+// float product holds the same value as the double one and its truncation is
+// the same integer; no FP64 instruction is needed.  The bounds are the int32
+// range: every float >= -2^31 is > -2^31 - 1.
 __device__ __forceinline__ int snap16(float f)
 {
-    const double d = __dmul_rn((double)f, 16.0);
-    if (!(d > -2147483649.0 && d < 2147483648.0))
+    const float s = fmul(f, 16.0f);
+    if (!(s >= -2147483648.0f && s < 2147483648.0f))
         return (int)0x80000000;
-    return __double2int_rz(d);
+    return __float2int_rz(s);
 }
 
 // Clipper::ComputeClipCode (Clipper.h:48-68).
@@ -188,13 +192,17 @@ static __device__ __noinline__ int clip_polygon(PolyVert* poly, uint32_t planeCo
 }
 
 // Reject / accept corner of one edge from the sign of B / float(C) and of C
-// (RasterTriangle.h:66-150); packed as rej | acc << 2.
+// (RasterTriangle.h:66-150); packed as rej | acc << 2.  The quotient of two
+// converted ints is never rounded to zero and keeps the sign of B*C, so
+// "slope >= 0" is decided exactly without a division: true when B == 0 and
+// C != 0 (+-0), when C == 0 and B > 0 (+inf), or when B and C have the same
+// sign; 0/0 is NaN and compares false.
 __device__ __forceinline__ uint32_t corner_code(int B, int C)
 {
-    const float slope = fdiv(__int2float_rn(B), __int2float_rn(C));
-    const bool cpos = __int2float_rn(C) >= 0.0f;
+    const bool cpos = C >= 0;
+    const bool slope_nonneg = (B == 0) ? (C != 0) : ((B > 0) == cpos);
     uint32_t rej, acc;
-    if (slope >= 0.0f) { rej = cpos ? 3u : 0u; acc = cpos ? 0u : 3u; }
+    if (slope_nonneg) { rej = cpos ? 3u : 0u; acc = cpos ? 0u : 3u; }
     else { rej = cpos ? 2u : 1u; acc = cpos ? 1u : 2u; }
     return rej | (acc << 2);
 }
@@ -210,7 +218,7 @@ __device__ __forceinline__ bool setup_triangle(const FrameDesc& f, float4 c0, fl
 #pragma unroll
     for (int k = 0; k < 3; k++)
     {
-        const float invW = fdiv(1.0f, cs[k].w);
+        const float invW = __frcp_rn(cs[k].w);  // == 1.0f / w, correctly rounded
         const float hx = fmul(cs[k].x, invW), hy = fmul(cs[k].y, invW), hz = fmul(cs[k].z, invW);
         float rx, ry;
         xform_point3(f.raster, hx, hy, hz, rx, ry);
@@ -228,7 +236,7 @@ __device__ __forceinline__ bool setup_triangle(const FrameDesc& f, float4 c0, fl
     t.v0x = vx[0]; t.v0y = vy[0];
     t.v1x = vx[1]; t.v1y = vy[1];
     t.v2x = vx[2]; t.v2y = vy[2];
-    t.invDet = fdiv(1.0f, __int2float_rn(det));
+    t.invDet = __frcp_rn(__int2float_rn(det));
     t.z0 = zp[0]; t.z1 = zp[1]; t.z2 = zp[2];
     t.invW0 = iw[0]; t.invW1 = iw[1]; t.invW2 = iw[2];
     t.meta = corner_code(B0, C0) | (corner_code(B1, C1) << 4) | (corner_code(B2, C2) << 8);

@@ -102,7 +102,8 @@ struct PassArgs
     RTri* rtris;
     uint32_t rtri_capacity;
     ClipPoly* polys;
-    uint32_t poly_capacity;
+    uint32_t poly_capacity;  // also the capacity of clip_list
+    uint32_t* clip_list;     // input triangles (flattened) that straddle a clip plane
     uint32_t* tile_count;    // total_tiles + 1
     uint32_t* tile_offset;   // total_tiles + 1 (exclusive scan of padded counts)
     uint32_t* tile_cursor;   // total_tiles
@@ -110,7 +111,7 @@ struct PassArgs
     uint64_t bin_capacity;
     uint32_t* big_list;      // raster triangles with many tiles, binned by whole blocks
     uint32_t big_capacity;
-    uint32_t* counters;      // [0] raster tris, [1] polys, [2] big tris, [3] raster work queue
+    uint32_t* counters;      // [0] raster tris, [1] polys, [2] big tris, [3] raster work queue, [4] clip list
     DeviceStatus* status;
     float4* color;
     float* depth;

@@ -90,19 +90,35 @@ __device__ __forceinline__ void clip_triangle(const FrameDesc& f, float4 c0, flo
     }
 }
 
+// Appends n raster triangles for this lane with one atomic per warp; returns
+// the lane's first slot.  Every lane of the warp must call it.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, int n)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    int incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total > 0)
+        base = atomicAdd(counter, (uint32_t)total);
+    return __shfl_sync(0xffffffffu, base, 31) + (uint32_t)(incl - n);
+}
+
+// Setup of the triangles that need no clipping (all clip codes zero), one
+// thread per input triangle; triangles that straddle a clip plane are queued
+// for k_clip, triangles outside one plane are dropped (Clipper.h:103-109).
 __global__ void __launch_bounds__(256) k_setup(PassArgs a)
 {
     const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = gi < a.total_tris;
-    const uint32_t lane = threadIdx.x & 31;
-
     uint32_t fi = 0, tri = 0;
     int nOut = 0;
-    bool clipped = false;
-    float4 c0 = {}, c1 = {}, c2 = {};
-    uint32_t planes = 0;
     RTri t;
-    if (active)
+    if (gi < a.total_tris)
     {
         fi = find_frame(a.frames, a.num_frames, gi, [](const FrameDesc& f) { return f.tri_base; });
         const FrameDesc& f = a.frames[fi];
@@ -117,87 +133,98 @@ __global__ void __launch_bounds__(256) k_setup(PassArgs a)
         }
         else
         {
-        c0 = a.clip[f.vtx_base + i0];
-        c1 = a.clip[f.vtx_base + i1];
-        c2 = a.clip[f.vtx_base + i2];
-        const uint32_t k0 = clip_code(c0), k1 = clip_code(c1), k2 = clip_code(c2);
-        if ((k0 | k1 | k2) == 0)
-        {
-            nOut = setup_triangle(f, c0, c1, c2, t) ? 1 : 0;
+            const float4 c0 = a.clip[f.vtx_base + i0];
+            const float4 c1 = a.clip[f.vtx_base + i1];
+            const float4 c2 = a.clip[f.vtx_base + i2];
+            const uint32_t k0 = clip_code(c0), k1 = clip_code(c1), k2 = clip_code(c2);
+            if ((k0 | k1 | k2) == 0)
+                nOut = setup_triangle(f, c0, c1, c2, t) ? 1 : 0;
+            else if (!(k0 & k1 & k2))
+            {
+                const uint32_t q = atomicAdd(&a.counters[4], 1u);
+                if (q < a.poly_capacity)
+                    a.clip_list[q] = gi;
+            }
         }
-        else if (!(k0 & k1 & k2))
+    }
+    const uint32_t base = warp_append(&a.counters[0], nOut);
+    if (nOut == 0)
+        return;
+    if (base >= a.rtri_capacity)
+    {
+        atomicOr(&a.status->overflow, 2u);
+        return;
+    }
+    t.order = tri << 4;
+    t.meta |= fi << 12;
+    t.poly = kUnclipped;
+    a.rtris[base] = t;
+}
+
+// Clipping of the queued triangles (Clipper.h:107-171): Sutherland-Hodgman,
+// fan triangulation, setup of each fan triangle.  Grid-stride over the queue.
+__global__ void __launch_bounds__(128) k_clip(PassArgs a)
+{
+    const uint32_t nq = min(*(volatile uint32_t*)&a.counters[4], a.poly_capacity);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (nq + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; r++)
+    {
+        const uint32_t q = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        PolyVert poly[kMaxPolygon];
+        float4 vc[kMaxPolygon];
+        int n = 0, nOut = 0;
+        uint32_t gi = 0, fi = 0, tri = 0;
+        if (q < nq)
         {
-            clipped = true;
-            planes = (k0 ^ k1) | (k1 ^ k2) | (k2 ^ k0);
-            PolyVert poly[kMaxPolygon];
-            float4 vc[kMaxPolygon];
-            int n;
-            clip_triangle(f, c0, c1, c2, planes, poly, n, vc);
+            gi = a.clip_list[q];
+            fi = find_frame(a.frames, a.num_frames, gi, [](const FrameDesc& f) { return f.tri_base; });
+            const FrameDesc& f = a.frames[fi];
+            tri = gi - f.tri_base;
+            const float4 c0 = a.clip[f.vtx_base + __ldg(f.indices + 3 * (size_t)tri)];
+            const float4 c1 = a.clip[f.vtx_base + __ldg(f.indices + 3 * (size_t)tri + 1)];
+            const float4 c2 = a.clip[f.vtx_base + __ldg(f.indices + 3 * (size_t)tri + 2)];
+            const uint32_t k0 = clip_code(c0), k1 = clip_code(c1), k2 = clip_code(c2);
+            clip_triangle(f, c0, c1, c2, (k0 ^ k1) | (k1 ^ k2) | (k2 ^ k0), poly, n, vc);
             for (int k = 2; k < n; k++)
             {
                 RTri tmp;
                 nOut += setup_triangle(f, vc[0], vc[k - 1], vc[k], tmp) ? 1 : 0;
             }
         }
-        }
-    }
-    // warp-aggregated append
-    int incl = nOut;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        const int v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= (uint32_t)o) incl += v;
-    }
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    uint32_t base = 0;
-    if (lane == 31 && total > 0)
-        base = atomicAdd(&a.counters[0], (uint32_t)total);
-    base = __shfl_sync(0xffffffffu, base, 31) + (uint32_t)(incl - nOut);
-    if (nOut == 0)
-        return;
-    if (base + (uint32_t)nOut > a.rtri_capacity)
-    {
-        atomicOr(&a.status->overflow, 2u);
-        return;
-    }
-    if (!clipped)
-    {
-        t.order = tri << 4;
-        t.meta |= fi << 12;
-        t.poly = kUnclipped;
-        a.rtris[base] = t;
-        return;
-    }
-    const FrameDesc& f = a.frames[fi];
-    PolyVert poly[kMaxPolygon];
-    float4 vc[kMaxPolygon];
-    int n;
-    clip_triangle(f, c0, c1, c2, planes, poly, n, vc);
-    const uint32_t pi = atomicAdd(&a.counters[1], 1u);
-    if (pi >= a.poly_capacity)
-    {
-        atomicOr(&a.status->overflow, 4u);
-        return;
-    }
-    ClipPoly& P = a.polys[pi];
-    for (int j = 0; j < n; j++)
-    {
-        P.w[j][0] = poly[j].w0;
-        P.w[j][1] = poly[j].w1;
-        P.w[j][2] = poly[j].w2;
-    }
-    P.n = (uint32_t)n;
-    uint32_t out = base;
-    for (int k = 2; k < n; k++)
-    {
-        RTri tk;
-        if (!setup_triangle(f, vc[0], vc[k - 1], vc[k], tk))
+        uint32_t out = warp_append(&a.counters[0], nOut);
+        if (nOut == 0)
             continue;
-        tk.order = (tri << 4) | (uint32_t)(k - 2);
-        tk.meta |= fi << 12;
-        tk.poly = (pi << 4) | (uint32_t)k;
-        a.rtris[out++] = tk;
+        if (out + (uint32_t)nOut > a.rtri_capacity)
+        {
+            atomicOr(&a.status->overflow, 2u);
+            continue;
+        }
+        const FrameDesc& f = a.frames[fi];
+        const uint32_t pi = atomicAdd(&a.counters[1], 1u);
+        if (pi >= a.poly_capacity)
+        {
+            atomicOr(&a.status->overflow, 4u);
+            continue;
+        }
+        ClipPoly& P = a.polys[pi];
+        for (int j = 0; j < n; j++)
+        {
+            P.w[j][0] = poly[j].w0;
+            P.w[j][1] = poly[j].w1;
+            P.w[j][2] = poly[j].w2;
+        }
+        P.n = (uint32_t)n;
+        for (int k = 2; k < n; k++)
+        {
+            RTri tk;
+            if (!setup_triangle(f, vc[0], vc[k - 1], vc[k], tk))
+                continue;
+            tk.order = (tri << 4) | (uint32_t)(k - 2);
+            tk.meta |= fi << 12;
+            tk.poly = (pi << 4) | (uint32_t)k;
+            a.rtris[out++] = tk;
+        }
     }
 }
 
@@ -210,16 +237,27 @@ __device__ __forceinline__ void bin_tile(const PassArgs& a, const FrameDesc& f, 
                                          const Edges& e, const BinGeom& g, int tx, int ty)
 {
     const uint32_t d = tile_decision(t, e, g, f, tx, ty);
+    // Neighbouring triangles of a warp often land in the same tile: lanes
+    // with equal tiles share one atomic (the lowest lane issues it).
+    const uint32_t act = __activemask();
+    const uint32_t tile = d ? f.tile_base + (uint32_t)(ty * f.tdx + tx) : 0xFFFFFFFFu;
+    const uint32_t peers = __match_any_sync(act, tile);
     if (!d)
         return;
-    const uint32_t tile = f.tile_base + (uint32_t)(ty * f.tdx + tx);
+    const uint32_t lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
     if (Phase == 0)
     {
-        atomicAdd(&a.tile_count[tile], 1u);
+        if ((int)lane == leader)
+            atomicAdd(&a.tile_count[tile], (uint32_t)__popc(peers));
     }
     else
     {
-        const uint64_t pos = (uint64_t)a.tile_offset[tile] + atomicAdd(&a.tile_cursor[tile], 1u);
+        uint32_t base = 0;
+        if ((int)lane == leader)
+            base = atomicAdd(&a.tile_cursor[tile], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+        const uint64_t pos = (uint64_t)a.tile_offset[tile] + base;
         if (pos < a.bin_capacity)
             a.bins[pos] = (ri << 2) | d;
     }
@@ -381,8 +419,9 @@ __global__ void k_scan_add(PassArgs a, const uint32_t* block_sums, uint32_t nblo
         a.status->big_tris = a.counters[2];
         if (a.counters[0] > a.rtri_capacity)
             atomicOr(&a.status->overflow, 2u);
-        if (a.counters[1] > a.poly_capacity)
+        if (a.counters[1] > a.poly_capacity || a.counters[4] > a.poly_capacity)
             atomicOr(&a.status->overflow, 4u);
+        a.status->clipped_polys = max(a.counters[1], a.counters[4]);
         if (total > a.bin_capacity)
             atomicOr(&a.status->overflow, 1u);
         if (a.counters[2] > a.big_capacity)
@@ -395,27 +434,54 @@ __global__ void k_scan_add(PassArgs a, const uint32_t* block_sums, uint32_t nblo
 // one pixel and keeps the winner of the reference's sequential depth test as
 // a key: (depth, submission order) — for LEQUAL the last fragment with the
 // smallest depth wins, for LESS the first — so the bin needs no ordering.
+//
+// Work split: warp w owns the 8x4 pixel block at (8*(w&1), 4*(w>>1)).  Bin
+// entries are staged 256 at a time as tile-relative edge equations; each
+// warp then tests 32 staged entries at once (one per lane) for overlap with
+// its block and against its hierarchical depth bound, and walks only the
+// entries whose ballot bit is set.  A small triangle therefore costs one
+// warp, not all eight.
 struct __align__(16) StagedTri
 {
     int A0, D0, K0, A1;    // e0 = A0*lx + D0*ly + K0 (with bias); l1 = A1*lx + D1*ly + K1 (no bias)
     int D1, K1, A2, D2;
     int K2;
     uint32_t flags;        // region lx0|lx1<<5|ly0<<10|ly1<<15, accept<<20, bias1<<21, bias2<<22
-    float invDet, z0;
-    float z1, z2;
     uint32_t rank;         // order + 1
     uint32_t ri;           // raster triangle index
+    float invDet, z0, z1, z2;
 };
 
+constexpr uint32_t kEmptyRegion = 16u | (16u << 10);  // lx0 = ly0 = 16 > lx1 = ly1 = 0
+
+// Lower bound (as a depth key) of every depth the reference computes for the
+// triangle at a pixel it rasterizes, or 0 (never culled) when the triangle is
+// large enough for int32 edge values to wrap.  Without wraparound the
+// barycentrics of rasterized pixels are within a few ulps of [0, 1], so the
+// computed depth is at least min(z) minus a few ulps of the |z| sum.
+__device__ __forceinline__ uint32_t zmin_key(const RTri& t)
+{
+    const int minx = min(t.v0x, min(t.v1x, t.v2x)), maxx = max(t.v0x, max(t.v1x, t.v2x));
+    const int miny = min(t.v0y, min(t.v1y, t.v2y)), maxy = max(t.v0y, max(t.v1y, t.v2y));
+    const float wx = (float)maxx - (float)minx + 1024.0f, wy = (float)maxy - (float)miny + 1024.0f;
+    if (!(2.0f * wx * wy < 1073741824.0f))
+        return 0u;
+    const float zmin = fminf(t.z0, fminf(t.z1, t.z2));
+    const float margin = 2e-6f * (fabsf(t.z0) + fabsf(t.z1) + fabsf(t.z2)) + 1e-30f;
+    const float lo = zmin - margin;
+    return (lo == lo) ? depth_key(lo) : 0u;
+}
+
 __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uint32_t nr, int tileX, int tileY,
-                                          StagedTri& s)
+                                          StagedTri& s, uint32_t& zkey)
 {
     const uint32_t ri = entry >> 2;
     if (ri >= nr)
     {
         // never written by a consistent pass; an empty region keeps it inert
-        s.flags = 16u | (16u << 10);
+        s.flags = kEmptyRegion;
         s.ri = kNoTriangle;
+        zkey = 0xFFFFFFFFu;
         return;
     }
     const bool accept = (entry & 3u) == kDecisionAccept;
@@ -455,13 +521,18 @@ __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uin
     s.z0 = t.z0; s.z1 = t.z1; s.z2 = t.z2;
     s.rank = t.order + 1u;
     s.ri = ri;
+    zkey = zmin_key(t);
 }
 
 __global__ void __launch_bounds__(kRasterThreads) k_raster(PassArgs a)
 {
     __shared__ StagedTri st[kRasterThreads];
+    __shared__ uint32_t s_flags[kRasterThreads];
+    __shared__ uint32_t s_zkey[kRasterThreads];
     __shared__ uint32_t s_tile;
-    const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int bx = (int)(warp & 1u) * 8, by = (int)(warp >> 1) * 4;
+    const int lx = bx + (int)(lane & 7u), ly = by + (int)(lane >> 3);
     const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
     for (;;)
     {
@@ -485,43 +556,66 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassArgs a)
         // best = (depth key << 32) | (LEQUAL: ~rank, LESS: rank); clear depth 1.0
         uint64_t best = ((uint64_t)0xBF800000u << 32) | (less ? 0u : 0xFFFFFFFFu);
         uint32_t bestRi = kNoTriangle;
+        uint32_t wzmax = 0xBF800000u;  // largest depth key held by this warp's pixels
 
         for (uint32_t c = 0; c < count; c += kRasterThreads)
         {
             const uint32_t m = min((uint32_t)kRasterThreads, count - c);
             if (threadIdx.x < m)
-                stage_tri(a, a.bins[start + c + threadIdx.x], nr, tileX, tileY, st[threadIdx.x]);
-            __syncthreads();
-            for (uint32_t j = 0; j < m; j++)
             {
-                const uint32_t fl = st[j].flags;
-                const int lx0 = fl & 31, lx1 = (fl >> 5) & 31, ly0 = (fl >> 10) & 31, ly1 = (fl >> 15) & 31;
-                if (lx < lx0 || lx > lx1 || ly < ly0 || ly > ly1)
-                    continue;
-                const StagedTri& s = st[j];
-                const int l1 = wadd(wadd(wmul(s.A1, lx), wmul(s.D1, ly)), s.K1);
-                const int l2 = wadd(wadd(wmul(s.A2, lx), wmul(s.D2, ly)), s.K2);
-                if (!(fl & (1u << 20)))
+                uint32_t zk;
+                stage_tri(a, a.bins[start + c + threadIdx.x], nr, tileX, tileY, st[threadIdx.x], zk);
+                s_flags[threadIdx.x] = st[threadIdx.x].flags;
+                s_zkey[threadIdx.x] = zk;
+            }
+            __syncthreads();
+            for (uint32_t g = 0; g < m; g += 32)
+            {
+                const uint32_t jl = g + lane;
+                bool hit = false;
+                if (jl < m)
                 {
-                    const int e0 = wadd(wadd(wmul(s.A0, lx), wmul(s.D0, ly)), s.K0);
-                    const int e1 = wadd(l1, (fl & (1u << 21)) ? -1 : 0);
-                    const int e2 = wadd(l2, (fl & (1u << 22)) ? -1 : 0);
-                    if ((e0 | e1 | e2) < 0)
+                    const uint32_t fl = s_flags[jl];
+                    const int lx0 = fl & 31, lx1 = (fl >> 5) & 31, ly0 = (fl >> 10) & 31, ly1 = (fl >> 15) & 31;
+                    hit = lx0 <= bx + 7 && lx1 >= bx && ly0 <= by + 3 && ly1 >= by && s_zkey[jl] <= wzmax;
+                }
+                uint32_t todo = __ballot_sync(0xffffffffu, hit);
+                if (!todo)
+                    continue;
+                while (todo)
+                {
+                    const uint32_t j = g + (uint32_t)(__ffs(todo) - 1);
+                    todo &= todo - 1u;
+                    const StagedTri& s = st[j];
+                    const uint32_t fl = s.flags;
+                    const int lx0 = fl & 31, lx1 = (fl >> 5) & 31, ly0 = (fl >> 10) & 31, ly1 = (fl >> 15) & 31;
+                    if (lx < lx0 || lx > lx1 || ly < ly0 || ly > ly1)
                         continue;
+                    const int l1 = wadd(wadd(wmul(s.A1, lx), wmul(s.D1, ly)), s.K1);
+                    const int l2 = wadd(wadd(wmul(s.A2, lx), wmul(s.D2, ly)), s.K2);
+                    if (!(fl & (1u << 20)))
+                    {
+                        const int e0 = wadd(wadd(wmul(s.A0, lx), wmul(s.D0, ly)), s.K0);
+                        const int e1 = wadd(l1, (fl & (1u << 21)) ? -1 : 0);
+                        const int e2 = wadd(l2, (fl & (1u << 22)) ? -1 : 0);
+                        if ((e0 | e1 | e2) < 0)
+                            continue;
+                    }
+                    // TriangleSSE::CalcBarycentricCoord / GetDepth (RasterTriangle.h:324-337)
+                    const float L0 = fmul(__int2float_rn(l1), s.invDet);
+                    const float L1 = fmul(__int2float_rn(l2), s.invDet);
+                    const float L2 = fsub(fsub(1.0f, L0), L1);
+                    const float d = fadd(fadd(fmul(L0, s.z0), fmul(L1, s.z1)), fmul(L2, s.z2));
+                    if (d != d)
+                        continue;
+                    const uint64_t key = ((uint64_t)depth_key(d) << 32) | (less ? s.rank : ~s.rank);
+                    if (key < best)
+                    {
+                        best = key;
+                        bestRi = s.ri;
+                    }
                 }
-                // TriangleSSE::CalcBarycentricCoord / GetDepth (RasterTriangle.h:324-337)
-                const float L0 = fmul(__int2float_rn(l1), s.invDet);
-                const float L1 = fmul(__int2float_rn(l2), s.invDet);
-                const float L2 = fsub(fsub(1.0f, L0), L1);
-                const float d = fadd(fadd(fmul(L0, s.z0), fmul(L1, s.z1)), fmul(L2, s.z2));
-                if (d != d)
-                    continue;
-                const uint64_t key = ((uint64_t)depth_key(d) << 32) | (less ? s.rank : ~s.rank);
-                if (key < best)
-                {
-                    best = key;
-                    bestRi = s.ri;
-                }
+                wzmax = __reduce_max_sync(0xffffffffu, (uint32_t)(best >> 32));
             }
             __syncthreads();
         }
@@ -607,7 +701,10 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
         k_vertex<<<(a.total_vertices + 255) / 256, 256, 0, s>>>(a);
     mark(1);
     if (a.total_tris)
+    {
         k_setup<<<(a.total_tris + 255) / 256, 256, 0, s>>>(a);
+        k_clip<<<sms * 4, 128, 0, s>>>(a);
+    }
     mark(2);
     k_bin<0><<<sms * 8, 256, 0, s>>>(a);
     k_bin_big<0><<<sms * 4, 256, 0, s>>>(a);
@@ -626,7 +723,7 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
 
 int kernels_per_pass(const PassArgs& a)
 {
-    return 9 + (a.total_vertices ? 1 : 0) + (a.total_tris ? 1 : 0);
+    return 9 + (a.total_vertices ? 1 : 0) + (a.total_tris ? 2 : 0);
 }
 
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s)

@@ -55,7 +55,8 @@ constexpr size_t kOffFrame = 0;
 constexpr size_t kOffClip = align256(kOffFrame + sizeof(FrameDesc));
 constexpr size_t kOffRtri = align256(kOffClip + sizeof(float4) * kMaxVertices);
 constexpr size_t kOffPoly = align256(kOffRtri + sizeof(RTri) * (size_t)kRtriCap);
-constexpr size_t kOffCount = align256(kOffPoly + sizeof(ClipPoly) * (size_t)kPolyCap);
+constexpr size_t kOffClipList = align256(kOffPoly + sizeof(ClipPoly) * (size_t)kPolyCap);
+constexpr size_t kOffCount = align256(kOffClipList + 4 * (size_t)kPolyCap);
 constexpr size_t kOffOffset = align256(kOffCount + 4 * (size_t)(kMaxTiles + 1));
 constexpr size_t kOffCursor = align256(kOffOffset + 4 * (size_t)(kMaxTiles + 1));
 constexpr size_t kOffBins = align256(kOffCursor + 4 * (size_t)(kMaxTiles + 1 + 8));
@@ -244,6 +245,7 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
     a.rtris = reinterpret_cast<RTri*>(base + kOffRtri);
     a.rtri_capacity = kRtriCap;
     a.polys = reinterpret_cast<ClipPoly*>(base + kOffPoly);
+    a.clip_list = reinterpret_cast<uint32_t*>(base + kOffClipList);
     a.poly_capacity = kPolyCap;
     a.tile_count = reinterpret_cast<uint32_t*>(base + kOffCount);
     a.tile_offset = reinterpret_cast<uint32_t*>(base + kOffOffset);

@@ -116,6 +116,9 @@ def reference_gradients(mesh, light, ks, shininess, views, ids, grad_color, shad
     col = shade_visible(pos, nrm, alb, mesh.indices, lt, k, s, views, ids, shader)
     g = torch.as_tensor(np.asarray(grad_color, np.float64)[..., :3])
     (col * g).sum().backward()
+    def scalar(t):  # shaders without a specular term leave ks/shininess unused
+        return 0.0 if t.grad is None else float(t.grad)
+
     return {"albedo": alb.grad.numpy(), "normals": nrm.grad.numpy(), "positions": pos.grad.numpy(),
-            "light": lt.grad.numpy(), "ks": float(k.grad), "shininess": float(s.grad),
+            "light": lt.grad.numpy(), "ks": scalar(k), "shininess": scalar(s),
             "color": col.detach().numpy()}
