@@ -415,6 +415,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.color = r->color.as<float4>();
     a.depth = r->depth.as<float>();
     a.tri_id = r->tri_id.as<uint32_t>();
+    a.total_pixels = pixels;
     a.num_sms = r->num_sms;
 
     EDXR_CUDA(run_pass(r, a));

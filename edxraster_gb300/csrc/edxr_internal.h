@@ -115,7 +115,8 @@ struct PassArgs
     DeviceStatus* status;
     float4* color;
     float* depth;
-    uint32_t* tri_id;
+    uint32_t* tri_id;        // raster writes the winning record index here, k_shade the input-triangle id
+    uint64_t total_pixels;   // frames * width * height
     int num_sms;
 };
 

@@ -230,17 +230,18 @@ __global__ void __launch_bounds__(128) k_clip(PassArgs a)
 
 // -------------------------------------------------------------------------
 // Binning.  Phase 0 counts the non-rejected (triangle, tile) pairs per tile,
-// phase 1 writes entries (raster triangle << 2 | decision).  Triangles with
-// more than kBigTiles candidate tiles are binned by a whole block each.
+// phase 1 writes entries (raster triangle << 2 | decision).  Triangles the
+// reference treats as small go through a lean per-thread path; the others
+// are binned by one warp each with the full decision of tile_decision.
+//
+// bin_emit counts or writes one entry for `tile` (decision d; nothing when
+// d is 0).  Neighbouring triangles of a warp often land in the same tile:
+// lanes with equal tiles share one atomic, issued by the lowest lane.
 template <int Phase>
-__device__ __forceinline__ void bin_tile(const PassArgs& a, const FrameDesc& f, uint32_t ri, const RTri& t,
-                                         const Edges& e, const BinGeom& g, int tx, int ty)
+__device__ __forceinline__ void bin_emit(const PassArgs& a, uint32_t ri, uint32_t d, uint32_t tile_in)
 {
-    const uint32_t d = tile_decision(t, e, g, f, tx, ty);
-    // Neighbouring triangles of a warp often land in the same tile: lanes
-    // with equal tiles share one atomic (the lowest lane issues it).
     const uint32_t act = __activemask();
-    const uint32_t tile = d ? f.tile_base + (uint32_t)(ty * f.tdx + tx) : 0xFFFFFFFFu;
+    const uint32_t tile = d ? tile_in : 0xFFFFFFFFu;
     const uint32_t peers = __match_any_sync(act, tile);
     if (!d)
         return;
@@ -264,6 +265,13 @@ __device__ __forceinline__ void bin_tile(const PassArgs& a, const FrameDesc& f, 
 }
 
 template <int Phase>
+__device__ __forceinline__ void bin_tile(const PassArgs& a, const FrameDesc& f, uint32_t ri, const RTri& t,
+                                         const Edges& e, const BinGeom& g, int tx, int ty)
+{
+    bin_emit<Phase>(a, ri, tile_decision(t, e, g, f, tx, ty), f.tile_base + (uint32_t)(ty * f.tdx + tx));
+}
+
+template <int Phase>
 __global__ void __launch_bounds__(256) k_bin(PassArgs a)
 {
     const uint32_t n = *(volatile uint32_t*)&a.counters[0];
@@ -273,11 +281,9 @@ __global__ void __launch_bounds__(256) k_bin(PassArgs a)
         const RTri t = a.rtris[ri];
         const FrameDesc& f = a.frames[t.meta >> 12];
         const BinGeom g = bin_geom(t, f);
-        const int nx = g.t16x1 - g.t16x0 + 1, ny = g.t16y1 - g.t16y0 + 1;
-        if (nx <= 0 || ny <= 0)
-            continue;
-        if (nx * ny > kBigTiles)
+        if (!g.small)
         {
+            // bounding box over 2x2 reference tiles: binned warp-cooperatively
             if (Phase == 0)
             {
                 const uint32_t b = atomicAdd(&a.counters[2], 1u);
@@ -286,18 +292,27 @@ __global__ void __launch_bounds__(256) k_bin(PassArgs a)
             }
             continue;
         }
-        const Edges e = tri_edges(t);
-        for (int ty = g.t16y0; ty <= g.t16y1; ty++)
-            for (int tx = g.t16x0; tx <= g.t16x1; tx++)
-                bin_tile<Phase>(a, f, ri, t, e, g, tx, ty);
+        // The reference rasterizes a small triangle with FineRasterize in every
+        // tile of its range (Renderer.cpp:173-180), so the decision is "fine"
+        // exactly where the quad-aligned bounding box meets the screen.
+        const int x0 = max(g.bbx0 & ~1, 0), x1 = min(g.bbx1 | 1, f.width - 1);
+        const int y0 = max(g.bby0 & ~1, 0), y1 = min(g.bby1 | 1, f.height - 1);
+        if (x0 > x1 || y0 > y1)
+            continue;
+        for (int ty = y0 >> kTileLog2; ty <= (y1 >> kTileLog2); ty++)
+            for (int tx = x0 >> kTileLog2; tx <= (x1 >> kTileLog2); tx++)
+                bin_emit<Phase>(a, ri, kDecisionFine, f.tile_base + (uint32_t)(ty * f.tdx + tx));
     }
 }
 
+// One warp per triangle of the big list; lanes take candidate tiles.
 template <int Phase>
 __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
 {
     const uint32_t nb = min(*(volatile uint32_t*)&a.counters[2], a.big_capacity);
-    for (uint32_t b = blockIdx.x; b < nb; b += gridDim.x)
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nb; b += nw)
     {
         const uint32_t ri = a.big_list[b];
         const RTri t = a.rtris[ri];
@@ -305,7 +320,7 @@ __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
         const BinGeom g = bin_geom(t, f);
         const Edges e = tri_edges(t);
         const int nx = g.t16x1 - g.t16x0 + 1, ny = g.t16y1 - g.t16y0 + 1;
-        for (int j = threadIdx.x; j < nx * ny; j += blockDim.x)
+        for (int j = (int)lane; j < nx * ny; j += 32)
             bin_tile<Phase>(a, f, ri, t, e, g, g.t16x0 + j % nx, g.t16y0 + j / nx);
     }
 }
@@ -620,35 +635,47 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassArgs a)
             __syncthreads();
         }
 
-        // epilogue: shade the winner, one write of colour, depth and id
+        // the winner's raster-triangle index, resolved and shaded by k_shade
         const int px = (tileX << 4) + lx, py = (tileY << 4) + ly;
         if (px < f.width && py < f.height)
-        {
-            const uint64_t o = f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px;
-            if (bestRi != kNoTriangle)
-            {
-                const RTri t = a.rtris[bestRi];
-                const Edges e = tri_edges(t);
-                const int cx = (px << 4) + 8, cy = (py << 4) + 8;
-                const int n1 = wadd(wmul(e.B[1], wsub(cx, t.v2x)), wmul(e.C[1], wsub(cy, t.v2y)));
-                const int n2 = wadd(wmul(e.B[2], wsub(cx, t.v2x)), wmul(e.C[2], wsub(cy, t.v2y)));
-                const float L0 = fmul(__int2float_rn(n1), t.invDet);
-                const float L1 = fmul(__int2float_rn(n2), t.invDet);
-                const float L2 = fsub(fsub(1.0f, L0), L1);
-                const float d = fadd(fadd(fmul(L0, t.z0), fmul(L1, t.z1)), fmul(L2, t.z2));
-                const float3 c = shade_fragment(f, t, a.polys, L0, L1);
-                a.color[o] = make_float4(c.x, c.y, c.z, 1.0f);
-                a.depth[o] = d;
-                a.tri_id[o] = t.order >> 4;
-            }
-            else
-            {
-                a.color[o] = make_float4(0.f, 0.f, 0.f, 0.f);
-                a.depth[o] = 1.0f;
-                a.tri_id[o] = kNoTriangle;
-            }
-        }
+            a.tri_id[f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px] = bestRi;
     }
+}
+
+// Deferred shading of the winners (Renderer.cpp:272-350 shades every
+// fragment and keeps the last; only the winner is shaded here): one thread
+// per pixel recomputes the winner's barycentrics and depth exactly
+// (RasterTriangle.h:324-337), interpolates and shades, and writes colour,
+// depth and the input-triangle id once.
+__global__ void __launch_bounds__(256) k_shade(PassArgs a)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.total_pixels)
+        return;
+    const uint32_t ri = a.tri_id[i];
+    if (ri == kNoTriangle || ri >= a.rtri_capacity)
+    {
+        a.color[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        a.depth[i] = 1.0f;
+        a.tri_id[i] = kNoTriangle;
+        return;
+    }
+    const RTri t = a.rtris[ri];
+    const FrameDesc& f = a.frames[t.meta >> 12];
+    const uint64_t local = i - f.pix_base;
+    const int px = (int)(local % (uint32_t)f.width), py = (int)(local / (uint32_t)f.width);
+    const Edges e = tri_edges(t);
+    const int cx = (px << 4) + 8, cy = (py << 4) + 8;
+    const int n1 = wadd(wmul(e.B[1], wsub(cx, t.v2x)), wmul(e.C[1], wsub(cy, t.v2y)));
+    const int n2 = wadd(wmul(e.B[2], wsub(cx, t.v2x)), wmul(e.C[2], wsub(cy, t.v2y)));
+    const float L0 = fmul(__int2float_rn(n1), t.invDet);
+    const float L1 = fmul(__int2float_rn(n2), t.invDet);
+    const float L2 = fsub(fsub(1.0f, L0), L1);
+    const float d = fadd(fadd(fmul(L0, t.z0), fmul(L1, t.z1)), fmul(L2, t.z2));
+    const float3 c = shade_fragment(f, t, a.polys, L0, L1);
+    a.color[i] = make_float4(c.x, c.y, c.z, 1.0f);
+    a.depth[i] = d;
+    a.tri_id[i] = t.order >> 4;
 }
 
 // -------------------------------------------------------------------------
@@ -717,13 +744,15 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
     k_bin_big<1><<<sms * 4, 256, 0, s>>>(a);
     mark(5);
     k_raster<<<raster_blocks(sms), kRasterThreads, 0, s>>>(a);
+    if (a.total_pixels)
+        k_shade<<<(unsigned)((a.total_pixels + 255) / 256), 256, 0, s>>>(a);
     mark(6);
     return cudaGetLastError();
 }
 
 int kernels_per_pass(const PassArgs& a)
 {
-    return 9 + (a.total_vertices ? 1 : 0) + (a.total_tris ? 2 : 0);
+    return 9 + (a.total_vertices ? 1 : 0) + (a.total_tris ? 2 : 0) + (a.total_pixels ? 1 : 0);
 }
 
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s)

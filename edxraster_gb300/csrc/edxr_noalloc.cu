@@ -259,6 +259,7 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
     a.color = reinterpret_cast<float4*>(color);
     a.depth = depth;
     a.tri_id = triangle_id;
+    a.total_pixels = (uint64_t)width * height;
     a.num_sms = sms;
 
     // The descriptor travels from this stack frame; a pageable source makes
