@@ -121,7 +121,7 @@ struct PassArgs
 };
 
 // Host-side launchers (edxr_kernels.cu).
-constexpr int kStageEvents = 7;  // boundaries of the 6 timed stages
+constexpr int kStageEvents = 8;  // boundaries of the 7 timed stages
 // ev: NULL, or kStageEvents events recorded around the stages.
 cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev = nullptr);
 int kernels_per_pass(const PassArgs& a);

@@ -744,9 +744,10 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
     k_bin_big<1><<<sms * 4, 256, 0, s>>>(a);
     mark(5);
     k_raster<<<raster_blocks(sms), kRasterThreads, 0, s>>>(a);
+    mark(6);
     if (a.total_pixels)
         k_shade<<<(unsigned)((a.total_pixels + 255) / 256), 256, 0, s>>>(a);
-    mark(6);
+    mark(7);
     return cudaGetLastError();
 }
 

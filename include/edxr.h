@@ -190,7 +190,8 @@ edxr_status edxr_get_stats(edxr_renderer* r, edxr_stats* stats);
  * without graph replay and CUDA events are recorded on the renderer's stream
  * around its stages:
  *   0 clear + vertex transform, 1 clip + setup, 2 bin count, 3 bin scan,
- *   4 bin scatter, 5 raster + shade.
+ *   4 bin scatter, 5 raster (coverage, depth test, winner), 6 shade (deferred
+ *   shading and the output writes).
  * edxr_get_stage_times synchronizes and writes the last pass's milliseconds
  * per stage into ms[0..*count-1] (capacity given in *count on entry). */
 edxr_status edxr_set_profiling(edxr_renderer* r, int enable);
