@@ -147,7 +147,7 @@ struct edxr_renderer
     Camera cam;
 
     DevBuf frames, clip, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, bins, big_list, counters, status;
-    DevBuf color, depth, tri_id, back8, diff_scratch;
+    DevBuf color, depth, tri_id, back8, diff_scratch, tri_first;
     uint64_t bin_capacity = 0, rtri_cap = 0, poly_cap = 0, big_cap = 0;
     uint64_t debug_cap = 0;  // EDXR_DEBUG_CAPACITY: tiny starting capacities (tests)
     std::vector<MeshStage> stage;
@@ -374,6 +374,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     const uint64_t nscan = (tiles + 4095) / 4096;
     EDXR_CUDA(r->frames.ensure(sizeof(FrameDesc) * n));
     EDXR_CUDA(r->clip.ensure(sizeof(float4) * std::max<uint64_t>(tv, 1)));
+    EDXR_CUDA(r->tri_first.ensure(4 * std::max<uint64_t>(tt, 1)));
     EDXR_CUDA(r->rtris.ensure(sizeof(RTri) * rcap));
     EDXR_CUDA(r->polys.ensure(sizeof(ClipPoly) * pcap));
     EDXR_CUDA(r->clip_list.ensure(4 * pcap));
@@ -415,6 +416,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.color = r->color.as<float4>();
     a.depth = r->depth.as<float>();
     a.tri_id = r->tri_id.as<uint32_t>();
+    a.tri_first = r->tri_first.as<uint32_t>();
     a.total_pixels = pixels;
     a.num_sms = r->num_sms;
 
@@ -582,7 +584,7 @@ edxr_status edxr_destroy(edxr_renderer* r)
         cudaGraphExecDestroy(r->graph);
     DevBuf* bufs[] = { &r->frames, &r->clip, &r->rtris, &r->polys, &r->clip_list, &r->tile_count, &r->tile_offset,
                        &r->tile_cursor, &r->bins, &r->big_list, &r->counters, &r->status, &r->color,
-                       &r->depth, &r->tri_id, &r->back8, &r->diff_scratch };
+                       &r->depth, &r->tri_id, &r->back8, &r->diff_scratch, &r->tri_first };
     for (DevBuf* b : bufs)
         b->release();
     for (auto& s : r->stage)

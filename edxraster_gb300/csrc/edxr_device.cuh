@@ -577,6 +577,19 @@ __device__ __forceinline__ float3 shade_fragment(const FrameDesc& f, const RTri&
     return shade_model(f, P, N, A);
 }
 
+// Frame owning output pixel i (binary search over pix_base).
+__device__ __forceinline__ uint32_t frame_of_pixel64(const FrameDesc* frames, uint32_t n, uint64_t p)
+{
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi)
+    {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (frames[mid].pix_base <= p) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // Frame owning flattened index i, by binary search over a monotone base
 // field (tri_base or tile_base) of the frame array.
 template <typename Get>

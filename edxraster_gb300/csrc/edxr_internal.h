@@ -113,9 +113,10 @@ struct PassArgs
     uint32_t big_capacity;
     uint32_t* counters;      // [0] raster tris, [1] polys, [2] big tris, [3] raster work queue, [4] clip list
     DeviceStatus* status;
+    uint32_t* tri_first;     // per flattened input triangle: its first raster triangle (or kNoTriangle)
     float4* color;
     float* depth;
-    uint32_t* tri_id;        // raster writes the winning record index here, k_shade the input-triangle id
+    uint32_t* tri_id;        // raster writes the winner's rank (order + 1, 0 = none) here, k_shade the input-triangle id
     uint64_t total_pixels;   // frames * width * height
     int num_sms;
 };

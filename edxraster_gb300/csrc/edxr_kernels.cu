@@ -8,16 +8,17 @@
 //                  and the post-pass, per input triangle        RasterTriangle.h:27-153
 //   k_bin*         (triangle, 16x16 tile) decisions, counted,   Renderer.cpp:161-229
 //                  scanned and scattered into per-tile bins
-//   k_raster       persistent tiles: coverage, depth, winner,   Renderer.cpp:248-350,
-//                  deferred shading of the winner, one write    Rasterizer.h:32-415
-//                  of colour, depth and triangle id per pixel   FrameBuffer.cpp:54-68
+//   k_raster       persistent tiles: coverage, depth test and   Renderer.cpp:248-270,
+//                  winner per pixel                             Rasterizer.h:32-415,
+//                                                               FrameBuffer.cpp:54-68
+//   k_shade        deferred shading of the winner; one write    Renderer.cpp:272-350
+//                  of colour, depth and triangle id per pixel
 #include <cuda_runtime.h>
 
 #include "edxr_device.cuh"
 
 namespace edxr {
 
-constexpr int kBigTiles = 64;          // candidate tiles above which a whole block bins a triangle
 constexpr int kRasterThreads = 256;    // one thread per pixel of a 16x16 tile
 constexpr int kScanItems = 4;
 constexpr int kScanThreads = 1024;
@@ -148,6 +149,8 @@ __global__ void __launch_bounds__(256) k_setup(PassArgs a)
         }
     }
     const uint32_t base = warp_append(&a.counters[0], nOut);
+    if (gi < a.total_tris)
+        a.tri_first[gi] = (nOut && base < a.rtri_capacity) ? base : kNoTriangle;  // k_clip sets clipped ones
     if (nOut == 0)
         return;
     if (base >= a.rtri_capacity)
@@ -215,6 +218,8 @@ __global__ void __launch_bounds__(128) k_clip(PassArgs a)
             P.w[j][2] = poly[j].w2;
         }
         P.n = (uint32_t)n;
+        // the surviving fan triangles are contiguous and in fan order
+        a.tri_first[gi] = out;
         for (int k = 2; k < n; k++)
         {
             RTri tk;
@@ -445,17 +450,22 @@ __global__ void k_scan_add(PassArgs a, const uint32_t* block_sums, uint32_t nblo
 }
 
 // -------------------------------------------------------------------------
-// Raster: persistent blocks take 16x16 tiles from a queue.  Each thread owns
-// one pixel and keeps the winner of the reference's sequential depth test as
-// a key: (depth, submission order) — for LEQUAL the last fragment with the
-// smallest depth wins, for LESS the first — so the bin needs no ordering.
-//
-// Work split: warp w owns the 8x4 pixel block at (8*(w&1), 4*(w>>1)).  Bin
-// entries are staged 256 at a time as tile-relative edge equations; each
-// warp then tests 32 staged entries at once (one per lane) for overlap with
-// its block and against its hierarchical depth bound, and walks only the
-// entries whose ballot bit is set.  A small triangle therefore costs one
-// warp, not all eight.
+// Raster: persistent blocks take 16x16 tiles from a queue.  The winner of
+// the reference's sequential depth test at a pixel is the fragment with the
+// smallest key (depth key << 32 | submission rank term): for LEQUAL the last
+// fragment with the smallest depth wins, for LESS the first.  Keys can be
+// combined in any order, so the bin needs no ordering and two paths can
+// share the work:
+//  * small entries (quad-aligned region of at most kSmallRegion pixels) are
+//    rasterized triangle-parallel by the thread that stages them, merging
+//    into a shared-memory key per pixel with a 64-bit atomicMin;
+//  * the other entries are staged as tile-relative edge equations and
+//    rasterized pixel-parallel: warp w owns the 8x4 block at
+//    (8*(w&1), 4*(w>>1)), tests 32 staged entries at once (one per lane) for
+//    overlap with its block and against its hierarchical depth bound, and
+//    walks only the entries whose ballot bit is set.
+// The pixel's final key is the minimum of both; its rank (order + 1, 0 when
+// nothing passed) goes to the id buffer for k_shade.
 struct __align__(16) StagedTri
 {
     int A0, D0, K0, A1;    // e0 = A0*lx + D0*ly + K0 (with bias); l1 = A1*lx + D1*ly + K1 (no bias)
@@ -463,11 +473,12 @@ struct __align__(16) StagedTri
     int K2;
     uint32_t flags;        // region lx0|lx1<<5|ly0<<10|ly1<<15, accept<<20, bias1<<21, bias2<<22
     uint32_t rank;         // order + 1
-    uint32_t ri;           // raster triangle index
+    uint32_t pad;
     float invDet, z0, z1, z2;
 };
 
 constexpr uint32_t kEmptyRegion = 16u | (16u << 10);  // lx0 = ly0 = 16 > lx1 = ly1 = 0
+constexpr int kSmallRegion = 32;
 
 // Lower bound (as a depth key) of every depth the reference computes for the
 // triangle at a pixel it rasterizes, or 0 (never culled) when the triangle is
@@ -487,6 +498,8 @@ __device__ __forceinline__ uint32_t zmin_key(const RTri& t)
     return (lo == lo) ? depth_key(lo) : 0u;
 }
 
+// Tile-relative edge equations, barycentric numerators and region of one
+// bin entry.
 __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uint32_t nr, int tileX, int tileY,
                                           StagedTri& s, uint32_t& zkey)
 {
@@ -495,7 +508,6 @@ __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uin
     {
         // never written by a consistent pass; an empty region keeps it inert
         s.flags = kEmptyRegion;
-        s.ri = kNoTriangle;
         zkey = 0xFFFFFFFFu;
         return;
     }
@@ -535,20 +547,49 @@ __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uin
     s.invDet = t.invDet;
     s.z0 = t.z0; s.z1 = t.z1; s.z2 = t.z2;
     s.rank = t.order + 1u;
-    s.ri = ri;
     zkey = zmin_key(t);
 }
 
-__global__ void __launch_bounds__(kRasterThreads) k_raster(PassArgs a)
+// Key of the fragment of staged triangle s at tile pixel (lx, ly), or false
+// when the pixel is not covered (FineRasterize's edge test; trivially
+// accepted entries skip it) or the depth is NaN (never passes).
+__device__ __forceinline__ bool fragment_key(const StagedTri& s, int lx, int ly, bool less, uint64_t& key)
+{
+    const uint32_t fl = s.flags;
+    const int l1 = wadd(wadd(wmul(s.A1, lx), wmul(s.D1, ly)), s.K1);
+    const int l2 = wadd(wadd(wmul(s.A2, lx), wmul(s.D2, ly)), s.K2);
+    if (!(fl & (1u << 20)))
+    {
+        const int e0 = wadd(wadd(wmul(s.A0, lx), wmul(s.D0, ly)), s.K0);
+        const int e1 = wadd(l1, (fl & (1u << 21)) ? -1 : 0);
+        const int e2 = wadd(l2, (fl & (1u << 22)) ? -1 : 0);
+        if ((e0 | e1 | e2) < 0)
+            return false;
+    }
+    // TriangleSSE::CalcBarycentricCoord / GetDepth (RasterTriangle.h:324-337)
+    const float L0 = fmul(__int2float_rn(l1), s.invDet);
+    const float L1 = fmul(__int2float_rn(l2), s.invDet);
+    const float L2 = fsub(fsub(1.0f, L0), L1);
+    const float d = fadd(fadd(fmul(L0, s.z0), fmul(L1, s.z1)), fmul(L2, s.z2));
+    if (d != d)
+        return false;
+    key = ((uint64_t)depth_key(d) << 32) | (less ? s.rank : ~s.rank);
+    return true;
+}
+
+__global__ void __launch_bounds__(kRasterThreads, 5) k_raster(PassArgs a)
 {
     __shared__ StagedTri st[kRasterThreads];
     __shared__ uint32_t s_flags[kRasterThreads];
     __shared__ uint32_t s_zkey[kRasterThreads];
+    __shared__ unsigned long long s_key[kRasterThreads];
     __shared__ uint32_t s_tile;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int bx = (int)(warp & 1u) * 8, by = (int)(warp >> 1) * 4;
     const int lx = bx + (int)(lane & 7u), ly = by + (int)(lane >> 3);
+    const uint32_t pix = (uint32_t)(ly * 16 + lx);  // this thread's pixel in s_key
     const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
+    s_key[pix] = ~0ull;
     for (;;)
     {
         if (threadIdx.x == 0)
@@ -568,20 +609,39 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassArgs a)
         if ((uint64_t)start + count > a.bin_capacity)
             count = 0;  // overflowed frame: rendered again by the host
 
-        // best = (depth key << 32) | (LEQUAL: ~rank, LESS: rank); clear depth 1.0
+        // clear depth 1.0 with no triangle: rank term ~0 (LEQUAL) or 0 (LESS)
         uint64_t best = ((uint64_t)0xBF800000u << 32) | (less ? 0u : 0xFFFFFFFFu);
-        uint32_t bestRi = kNoTriangle;
-        uint32_t wzmax = 0xBF800000u;  // largest depth key held by this warp's pixels
+        uint32_t wzmax = 0xBF800000u;  // largest depth key held in this warp's registers
 
         for (uint32_t c = 0; c < count; c += kRasterThreads)
         {
             const uint32_t m = min((uint32_t)kRasterThreads, count - c);
             if (threadIdx.x < m)
             {
+                StagedTri s;
                 uint32_t zk;
-                stage_tri(a, a.bins[start + c + threadIdx.x], nr, tileX, tileY, st[threadIdx.x], zk);
-                s_flags[threadIdx.x] = st[threadIdx.x].flags;
-                s_zkey[threadIdx.x] = zk;
+                stage_tri(a, a.bins[start + c + threadIdx.x], nr, tileX, tileY, s, zk);
+                const uint32_t fl = s.flags;
+                const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31, ry1 = (fl >> 15) & 31;
+                const int area = (rx1 - rx0 + 1) * (ry1 - ry0 + 1);
+                if (!(fl & (1u << 20)) && rx0 <= rx1 && ry0 <= ry1 && area <= kSmallRegion)
+                {
+                    // small: this thread rasterizes the triangle's few pixels
+                    for (int y = ry0; y <= ry1; y++)
+                        for (int x = rx0; x <= rx1; x++)
+                        {
+                            uint64_t key;
+                            if (fragment_key(s, x, y, less, key))
+                                atomicMin(&s_key[y * 16 + x], (unsigned long long)key);
+                        }
+                    s_flags[threadIdx.x] = kEmptyRegion;
+                }
+                else
+                {
+                    st[threadIdx.x] = s;
+                    s_flags[threadIdx.x] = fl;
+                    s_zkey[threadIdx.x] = zk;
+                }
             }
             __syncthreads();
             for (uint32_t g = 0; g < m; g += 32)
@@ -606,54 +666,54 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(PassArgs a)
                     const int lx0 = fl & 31, lx1 = (fl >> 5) & 31, ly0 = (fl >> 10) & 31, ly1 = (fl >> 15) & 31;
                     if (lx < lx0 || lx > lx1 || ly < ly0 || ly > ly1)
                         continue;
-                    const int l1 = wadd(wadd(wmul(s.A1, lx), wmul(s.D1, ly)), s.K1);
-                    const int l2 = wadd(wadd(wmul(s.A2, lx), wmul(s.D2, ly)), s.K2);
-                    if (!(fl & (1u << 20)))
-                    {
-                        const int e0 = wadd(wadd(wmul(s.A0, lx), wmul(s.D0, ly)), s.K0);
-                        const int e1 = wadd(l1, (fl & (1u << 21)) ? -1 : 0);
-                        const int e2 = wadd(l2, (fl & (1u << 22)) ? -1 : 0);
-                        if ((e0 | e1 | e2) < 0)
-                            continue;
-                    }
-                    // TriangleSSE::CalcBarycentricCoord / GetDepth (RasterTriangle.h:324-337)
-                    const float L0 = fmul(__int2float_rn(l1), s.invDet);
-                    const float L1 = fmul(__int2float_rn(l2), s.invDet);
-                    const float L2 = fsub(fsub(1.0f, L0), L1);
-                    const float d = fadd(fadd(fmul(L0, s.z0), fmul(L1, s.z1)), fmul(L2, s.z2));
-                    if (d != d)
-                        continue;
-                    const uint64_t key = ((uint64_t)depth_key(d) << 32) | (less ? s.rank : ~s.rank);
-                    if (key < best)
-                    {
+                    uint64_t key;
+                    if (fragment_key(s, lx, ly, less, key) && key < best)
                         best = key;
-                        bestRi = s.ri;
-                    }
                 }
                 wzmax = __reduce_max_sync(0xffffffffu, (uint32_t)(best >> 32));
             }
             __syncthreads();
         }
 
-        // the winner's raster-triangle index, resolved and shaded by k_shade
+        // both paths merged; the rank of the winner for k_shade
+        const uint64_t sk = s_key[pix];
+        s_key[pix] = ~0ull;  // ready for the next tile (its first barrier orders this)
+        if (sk < best)
+            best = sk;
+        const uint32_t low = (uint32_t)best;
+        const uint32_t rank = less ? low : ~low;
         const int px = (tileX << 4) + lx, py = (tileY << 4) + ly;
         if (px < f.width && py < f.height)
-            a.tri_id[f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px] = bestRi;
+            a.tri_id[f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px] = rank;
     }
 }
 
 // Deferred shading of the winners (Renderer.cpp:272-350 shades every
 // fragment and keeps the last; only the winner is shaded here): one thread
-// per pixel recomputes the winner's barycentrics and depth exactly
-// (RasterTriangle.h:324-337), interpolates and shades, and writes colour,
-// depth and the input-triangle id once.
+// per pixel finds the winner's raster triangle from its rank, recomputes its
+// barycentrics and depth exactly (RasterTriangle.h:324-337), interpolates and
+// shades, and writes colour, depth and the input-triangle id once.
 __global__ void __launch_bounds__(256) k_shade(PassArgs a)
 {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.total_pixels)
         return;
-    const uint32_t ri = a.tri_id[i];
-    if (ri == kNoTriangle || ri >= a.rtri_capacity)
+    const uint32_t rank = a.tri_id[i];
+    const FrameDesc& f = a.frames[frame_of_pixel64(a.frames, a.num_frames, i)];
+    const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
+    uint32_t ri = kNoTriangle;
+    if (rank != 0)
+    {
+        const uint32_t order = rank - 1u;
+        const uint32_t gi = f.tri_base + (order >> 4);
+        ri = gi < a.total_tris ? a.tri_first[gi] : kNoTriangle;
+        // a clipped triangle's fan pieces are contiguous, in fan order
+        for (int s = 0; s < kMaxPolygon && ri < nr && a.rtris[ri].order != order; s++)
+            ri++;
+        if (ri >= nr || a.rtris[ri].order != order)
+            ri = kNoTriangle;
+    }
+    if (ri == kNoTriangle)
     {
         a.color[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         a.depth[i] = 1.0f;
@@ -661,7 +721,6 @@ __global__ void __launch_bounds__(256) k_shade(PassArgs a)
         return;
     }
     const RTri t = a.rtris[ri];
-    const FrameDesc& f = a.frames[t.meta >> 12];
     const uint64_t local = i - f.pix_base;
     const int px = (int)(local % (uint32_t)f.width), py = (int)(local / (uint32_t)f.width);
     const Edges e = tri_edges(t);

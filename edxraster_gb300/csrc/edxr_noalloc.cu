@@ -63,7 +63,8 @@ constexpr size_t kOffBins = align256(kOffCursor + 4 * (size_t)(kMaxTiles + 1 + 8
 constexpr size_t kOffBig = align256(kOffBins + 4 * (size_t)kBinCap);
 constexpr size_t kOffCounters = align256(kOffBig + 4 * (size_t)kBigCap);
 constexpr size_t kOffStatus = align256(kOffCounters + 4 * 8);
-constexpr size_t kNoAllocScratchBytes = align256(kOffStatus + sizeof(DeviceStatus));
+constexpr size_t kOffTriFirst = align256(kOffStatus + sizeof(DeviceStatus));
+constexpr size_t kNoAllocScratchBytes = align256(kOffTriFirst + 4 * (size_t)kMaxTriangles);
 
 // The scratch of edxr_render_noalloc (about 12 MiB per device).  Host code
 // only ever sees a host-side stand-in for this name; its device address comes
@@ -259,6 +260,7 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
     a.color = reinterpret_cast<float4*>(color);
     a.depth = depth;
     a.tri_id = triangle_id;
+    a.tri_first = reinterpret_cast<uint32_t*>(base + kOffTriFirst);
     a.total_pixels = (uint64_t)width * height;
     a.num_sms = sms;
 
