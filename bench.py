@@ -226,13 +226,24 @@ def time_frames(r, stream, flush_l2, render, steps, warmup):
     return sum(s.elapsed_time(e) for s, e in zip(starts, ends))
 
 
-def measure_plain(sc, device, steps, warmup, flush_l2):
+def apply_tuning(r, workload):
+    """Launch tunables the autotuner stored for this workload on this GPU, if any."""
+    from edxraster_gb300 import autotune
+    t = autotune.load(workload)
+    if t:
+        r.SetTuning(t)
+    return t
+
+
+def measure_plain(sc, device, steps, warmup, flush_l2, workload=None):
     import torch
     from edxraster_gb300 import renderer as R
     stream = torch.cuda.Stream()
     r = R.Renderer(device=device, stream=stream)
     r.Initialize(sc.view.width, sc.view.height)
     R.configure(r, sc.view)
+    if workload:
+        apply_tuning(r, workload)
     dm = R.DeviceMesh.from_mesh(sc.mesh, device="cuda:%d" % device)
     ms = time_frames(r, stream, lambda: flush_l2(stream), lambda: r.RenderMesh(dm, synchronize=False),
                      steps, warmup) / steps
@@ -259,6 +270,7 @@ def measure_batched(device, steps, warmup, flush_l2):
     stream = torch.cuda.Stream()
     r = R.Renderer(device=device, stream=stream)
     r.Initialize(512, 512)
+    apply_tuning(r, "batched")
     batch = r.PrepareBatch(dms, views)
     ms_b = time_frames(r, stream, lambda: flush_l2(stream),
                        lambda: r.RenderBatched(batch, None, 512, 512, synchronize=False), steps, warmup) / steps
@@ -390,6 +402,7 @@ def run_gpu(args, world, rank, local):
     r = R.Renderer(device=local, stream=stream)
     r.Initialize(W, H)
     R.configure(r, sc.view)
+    tuning = apply_tuning(r, args.workload)
     dmesh = R.DeviceMesh.from_mesh(sc.mesh, device="cuda:%d" % local)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:%d" % local)
 
@@ -424,6 +437,7 @@ def run_gpu(args, world, rank, local):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     stats = r.Stats()
+    r_tuning = r.GetTuning()
     ms_per_step = total_ms / args.steps
     value = world * sc.mesh.nt * args.steps / (total_ms / 1e3) / 1e6
 
@@ -476,7 +490,8 @@ def run_gpu(args, world, rank, local):
                 flush.zero_()
         for wname in ("sphere", "stress"):
             if wname != args.workload:
-                per_config[wname] = measure_plain(WORKLOADS[wname][1](), local, max(3, args.steps // 4), 3, flush_on)
+                per_config[wname] = measure_plain(WORKLOADS[wname][1](), local, max(3, args.steps // 4), 3, flush_on,
+                                                  workload=wname)
         per_config["batched"] = measure_batched(local, 3, 3, flush_on)
         per_config["differentiable"] = measure_diff(local, 5, 3)
 
@@ -504,6 +519,7 @@ def run_gpu(args, world, rank, local):
         "e2e": {"value": e2e_value, "unit": "Mtris/s", "h2d_bytes_per_step": hmesh.nbytes(),
                 "d2h_bytes_per_step": W * H * PIXEL_BYTES},
         "gpu_launches": int(stats.kernels_per_pass) * args.steps,
+        "tuning": r_tuning,
         "clocks": clock_info,
         "raster_triangles": int(stats.raster_triangles), "bin_entries": int(stats.bin_entries),
         "cpu_baseline": cpu,

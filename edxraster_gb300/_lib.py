@@ -59,6 +59,12 @@ class Stats(ctypes.Structure):
                 ("kernels_per_pass", ctypes.c_uint32), ("clipped_polygons", ctypes.c_uint32)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("small_region", ctypes.c_int), ("raster_variant", ctypes.c_int),
+                ("bin_blocks_per_sm", ctypes.c_int), ("raster_blocks_per_sm", ctypes.c_int),
+                ("bin_entries_per_triangle", ctypes.c_uint32)]
+
+
 class View(ctypes.Structure):
     _fields_ = [("mesh", ctypes.c_uint32), ("mv", _f16), ("proj", _f16), ("raster", _f16),
                 ("shading", ShaderParams), ("ps_kind", ctypes.c_int), ("depth_func", ctypes.c_int)]
@@ -90,6 +96,8 @@ SIGNATURES = {
     "edxr_get_back_buffer": ([_P, ctypes.POINTER(_P)], ctypes.c_int),
     "edxr_get_stats": ([_P, ctypes.POINTER(Stats)], ctypes.c_int),
     "edxr_set_profiling": ([_P, ctypes.c_int], ctypes.c_int),
+    "edxr_set_tuning": ([_P, ctypes.POINTER(Tuning)], ctypes.c_int),
+    "edxr_get_tuning": ([_P, ctypes.POINTER(Tuning)], ctypes.c_int),
     "edxr_get_stage_times": ([_P, _P, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
     "edxr_last_error_string": ([], ctypes.c_char_p),
     "edxr_render_batched": ([_P, ctypes.POINTER(Mesh), ctypes.c_uint32, ctypes.POINTER(View), ctypes.c_uint32,

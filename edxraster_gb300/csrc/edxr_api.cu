@@ -173,6 +173,9 @@ struct edxr_renderer
     // stage timing
     bool profiling = false;
     cudaEvent_t stage_ev[kStageEvents] = {};
+
+    Tuning tuning = default_tuning();
+    uint32_t bins_per_tri = 2;
 };
 
 namespace {
@@ -366,8 +369,8 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     {
         r->poly_cap = std::max<uint64_t>({ r->poly_cap, std::max<uint64_t>(tt / 16, 65536) });
         r->big_cap = std::max<uint64_t>({ r->big_cap, std::max<uint64_t>(tt / 8, 65536) });
-        if (r->bin_capacity < 2 * tt + 4 * tiles)
-            r->bin_capacity = std::max<uint64_t>(2 * tt + 4 * tiles, 1u << 20);
+        if (r->bin_capacity < (uint64_t)r->bins_per_tri * tt + 4 * tiles)
+            r->bin_capacity = std::max<uint64_t>((uint64_t)r->bins_per_tri * tt + 4 * tiles, 1u << 20);
     }
     r->rtri_cap = std::min<uint64_t>(r->rtri_cap, 0xFFFFFFF0u);
     const uint64_t rcap = r->rtri_cap, pcap = r->poly_cap;
@@ -393,6 +396,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
 
     PassArgs a;
     std::memset(&a, 0, sizeof(a));
+    a.tune = r->tuning;
     a.frames = r->frames.as<FrameDesc>();
     a.num_frames = n;
     a.total_vertices = (uint32_t)tv;
@@ -765,6 +769,38 @@ edxr_status edxr_get_stats(edxr_renderer* r, edxr_stats* st)
     st->tile_size = kTileSize;
     st->kernels_per_pass = r->last_frames ? (uint32_t)kernels_per_pass(r->last) : 0u;
     st->clipped_polygons = r->status_host->clipped_polys;
+    return EDXR_OK;
+}
+
+edxr_status edxr_set_tuning(edxr_renderer* r, const edxr_tuning* t)
+{
+    if (!r || !t)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    if (t->small_region < 0 || t->small_region > 256 || (t->raster_variant != 0 && t->raster_variant != 1) ||
+        t->bin_blocks_per_sm < 1 || t->bin_blocks_per_sm > 64 || t->raster_blocks_per_sm < 0 ||
+        t->raster_blocks_per_sm > 32 || t->bin_entries_per_triangle < 1 || t->bin_entries_per_triangle > 1024)
+        return fail(EDXR_ERR_INVALID_ARG, "tuning value out of range");
+    DeviceGuard g(r->device);
+    edxr_status s = sync_pass(r);
+    if (s != EDXR_OK)
+        return s;
+    r->tuning.small_region = t->small_region;
+    r->tuning.raster_variant = t->raster_variant;
+    r->tuning.bin_blocks_per_sm = t->bin_blocks_per_sm;
+    r->tuning.raster_blocks_per_sm = t->raster_blocks_per_sm;
+    r->bins_per_tri = t->bin_entries_per_triangle;
+    return EDXR_OK;
+}
+
+edxr_status edxr_get_tuning(edxr_renderer* r, edxr_tuning* t)
+{
+    if (!r || !t)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    t->small_region = r->tuning.small_region;
+    t->raster_variant = r->tuning.raster_variant;
+    t->bin_blocks_per_sm = r->tuning.bin_blocks_per_sm;
+    t->raster_blocks_per_sm = r->tuning.raster_blocks_per_sm;
+    t->bin_entries_per_triangle = r->bins_per_tri;
     return EDXR_OK;
 }
 

@@ -90,9 +90,19 @@ struct DeviceStatus
     uint32_t pad;
 };
 
+// Tunables of one pass (edxr_set_tuning; chosen by the autotuner).
+struct Tuning
+{
+    int small_region;     // bin entries whose pixel region is at most this are rasterized triangle-parallel
+    int raster_variant;   // 0: k_raster without a register cap, 1: capped for 5 blocks per SM
+    int bin_blocks_per_sm;
+    int raster_blocks_per_sm;  // 0 = as many as fit
+};
+
 // Launch parameters shared by every kernel of one pass.
 struct PassArgs
 {
+    Tuning tune;
     const FrameDesc* frames;
     uint32_t num_frames;
     uint32_t total_vertices;
@@ -126,6 +136,7 @@ constexpr int kStageEvents = 8;  // boundaries of the 7 timed stages
 // ev: NULL, or kStageEvents events recorded around the stages.
 cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev = nullptr);
 int kernels_per_pass(const PassArgs& a);
+Tuning default_tuning();
 // Sets the message edxr_last_error_string returns on this thread.
 void record_error(const char* msg);
 void prepare_kernels();

@@ -456,7 +456,7 @@ __global__ void k_scan_add(PassArgs a, const uint32_t* block_sums, uint32_t nblo
 // fragment with the smallest depth wins, for LESS the first.  Keys can be
 // combined in any order, so the bin needs no ordering and two paths can
 // share the work:
-//  * small entries (quad-aligned region of at most kSmallRegion pixels) are
+//  * small entries (quad-aligned region of at most tune.small_region pixels) are
 //    rasterized triangle-parallel by the thread that stages them, merging
 //    into a shared-memory key per pixel with a 64-bit atomicMin;
 //  * the other entries are staged as tile-relative edge equations and
@@ -478,7 +478,6 @@ struct __align__(16) StagedTri
 };
 
 constexpr uint32_t kEmptyRegion = 16u | (16u << 10);  // lx0 = ly0 = 16 > lx1 = ly1 = 0
-constexpr int kSmallRegion = 32;
 
 // Lower bound (as a depth key) of every depth the reference computes for the
 // triangle at a pixel it rasterizes, or 0 (never culled) when the triangle is
@@ -577,7 +576,8 @@ __device__ __forceinline__ bool fragment_key(const StagedTri& s, int lx, int ly,
     return true;
 }
 
-__global__ void __launch_bounds__(kRasterThreads, 5) k_raster(PassArgs a)
+template <int MinBlocks>
+__global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a)
 {
     __shared__ StagedTri st[kRasterThreads];
     __shared__ uint32_t s_flags[kRasterThreads];
@@ -624,7 +624,7 @@ __global__ void __launch_bounds__(kRasterThreads, 5) k_raster(PassArgs a)
                 const uint32_t fl = s.flags;
                 const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31, ry1 = (fl >> 15) & 31;
                 const int area = (rx1 - rx0 + 1) * (ry1 - ry0 + 1);
-                if (!(fl & (1u << 20)) && rx0 <= rx1 && ry0 <= ry1 && area <= kSmallRegion)
+                if (!(fl & (1u << 20)) && rx0 <= rx1 && ry0 <= ry1 && area <= a.tune.small_region)
                 {
                     // small: this thread rasterizes the triangle's few pixels
                     for (int y = ry0; y <= ry1; y++)
@@ -757,20 +757,43 @@ __global__ void k_back_buffer(const float4* color, uchar4* out, int width, int h
 // -------------------------------------------------------------------------
 
 
-static int raster_blocks(int sms)
+static int raster_occupancy(int variant)
 {
-    static int per_sm = 0;
-    if (!per_sm)
+    static int per_sm[2] = { 0, 0 };
+    if (!per_sm[variant])
     {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster, kRasterThreads, 0) != cudaSuccess || per_sm < 1)
-            per_sm = 1;
+        const cudaError_t e = variant
+            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[1], k_raster<5>, kRasterThreads, 0)
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[0], k_raster<4>, kRasterThreads, 0);
+        if (e != cudaSuccess || per_sm[variant] < 1)
+            per_sm[variant] = 1;
     }
-    return sms * per_sm;
+    return per_sm[variant];
+}
+
+static int raster_blocks(int sms, const Tuning& t)
+{
+    const int variant = t.raster_variant ? 1 : 0;
+    int per = raster_occupancy(variant);
+    if (t.raster_blocks_per_sm > 0 && t.raster_blocks_per_sm < per)
+        per = t.raster_blocks_per_sm;
+    return sms * per;
 }
 
 void prepare_kernels()
 {
-    raster_blocks(1);
+    raster_occupancy(0);
+    raster_occupancy(1);
+}
+
+Tuning default_tuning()
+{
+    Tuning t;
+    t.small_region = 32;
+    t.raster_variant = 1;
+    t.bin_blocks_per_sm = 8;
+    t.raster_blocks_per_sm = 0;
+    return t;
 }
 
 cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
@@ -792,17 +815,21 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
         k_clip<<<sms * 4, 128, 0, s>>>(a);
     }
     mark(2);
-    k_bin<0><<<sms * 8, 256, 0, s>>>(a);
+    const int bin_blocks = sms * (a.tune.bin_blocks_per_sm > 0 ? a.tune.bin_blocks_per_sm : 8);
+    k_bin<0><<<bin_blocks, 256, 0, s>>>(a);
     k_bin_big<0><<<sms * 4, 256, 0, s>>>(a);
     mark(3);
     k_scan_blocks<<<nscan, kScanThreads, 0, s>>>(a, block_sums);
     k_scan_spine<<<1, 1024, 0, s>>>(block_sums, nscan);
     k_scan_add<<<(a.total_tiles + 255) / 256 + 1, 256, 0, s>>>(a, block_sums, nscan);
     mark(4);
-    k_bin<1><<<sms * 8, 256, 0, s>>>(a);
+    k_bin<1><<<bin_blocks, 256, 0, s>>>(a);
     k_bin_big<1><<<sms * 4, 256, 0, s>>>(a);
     mark(5);
-    k_raster<<<raster_blocks(sms), kRasterThreads, 0, s>>>(a);
+    if (a.tune.raster_variant)
+        k_raster<5><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
+    else
+        k_raster<4><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
     mark(6);
     if (a.total_pixels)
         k_shade<<<(unsigned)((a.total_pixels + 255) / 256), 256, 0, s>>>(a);

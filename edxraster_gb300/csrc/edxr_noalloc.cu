@@ -237,6 +237,7 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
 
     PassArgs a;
     memset(&a, 0, sizeof(a));
+    a.tune = default_tuning();
     a.frames = reinterpret_cast<const FrameDesc*>(base + kOffFrame);
     a.num_frames = 1;
     a.total_vertices = f.nv;

@@ -249,6 +249,20 @@ class Renderer:
         _lib.check(self._lib.edxr_get_stats(self._h, ctypes.byref(s)))
         return s
 
+    TUNING_FIELDS = ("small_region", "raster_variant", "bin_blocks_per_sm", "raster_blocks_per_sm",
+                     "bin_entries_per_triangle")
+
+    def SetTuning(self, tuning: dict):
+        cur = self.GetTuning()
+        cur.update({k: int(v) for k, v in tuning.items() if k in self.TUNING_FIELDS})
+        t = _lib.Tuning(*[cur[k] for k in self.TUNING_FIELDS])
+        _lib.check(self._lib.edxr_set_tuning(self._h, ctypes.byref(t)))
+
+    def GetTuning(self) -> dict:
+        t = _lib.Tuning()
+        _lib.check(self._lib.edxr_get_tuning(self._h, ctypes.byref(t)))
+        return {k: int(getattr(t, k)) for k in self.TUNING_FIELDS}
+
     STAGES = ("clear+vertex", "clip+setup", "bin count", "bin scan", "bin scatter", "raster", "shade")
 
     def SetProfiling(self, enable: bool):

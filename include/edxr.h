@@ -197,6 +197,22 @@ edxr_status edxr_get_stats(edxr_renderer* r, edxr_stats* stats);
 edxr_status edxr_set_profiling(edxr_renderer* r, int enable);
 edxr_status edxr_get_stage_times(edxr_renderer* r, float* ms, uint32_t* count);
 
+/* Launch tunables (no counterpart in the reference); they change speed only,
+ * never results.  The project's autotuner (edxraster_gb300/autotune.py)
+ * times candidates on a workload and stores the best as JSON. */
+typedef struct edxr_tuning
+{
+    int small_region;             /* bin entries whose pixel region in a 16x16 tile is at most this
+                                     many pixels are rasterized one triangle per thread; 0 disables */
+    int raster_variant;           /* 0: raster kernel without a register cap, 1: capped for 5 blocks per SM */
+    int bin_blocks_per_sm;        /* grid of the per-triangle binning kernels */
+    int raster_blocks_per_sm;     /* persistent raster blocks per SM; 0 = the occupancy maximum */
+    uint32_t bin_entries_per_triangle;  /* initial bin-buffer capacity per triangle (grows on overflow) */
+} edxr_tuning;
+
+edxr_status edxr_set_tuning(edxr_renderer* r, const edxr_tuning* tuning);
+edxr_status edxr_get_tuning(edxr_renderer* r, edxr_tuning* tuning);
+
 /* Message of the last failing call on this thread. */
 const char* edxr_last_error_string(void);
 
