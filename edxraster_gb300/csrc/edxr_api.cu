@@ -776,7 +776,7 @@ edxr_status edxr_set_tuning(edxr_renderer* r, const edxr_tuning* t)
 {
     if (!r || !t)
         return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
-    if (t->small_region < 0 || t->small_region > 256 || (t->raster_variant != 0 && t->raster_variant != 1) ||
+    if (t->small_region < 0 || t->small_region > 256 || t->raster_variant < 0 || t->raster_variant > 2 ||
         t->bin_blocks_per_sm < 1 || t->bin_blocks_per_sm > 64 || t->raster_blocks_per_sm < 0 ||
         t->raster_blocks_per_sm > 32 || t->bin_entries_per_triangle < 1 || t->bin_entries_per_triangle > 1024)
         return fail(EDXR_ERR_INVALID_ARG, "tuning value out of range");

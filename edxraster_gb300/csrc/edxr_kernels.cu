@@ -576,7 +576,7 @@ __device__ __forceinline__ bool fragment_key(const StagedTri& s, int lx, int ly,
     return true;
 }
 
-template <int MinBlocks>
+template <int MinBlocks, bool SmallPath>
 __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a)
 {
     __shared__ StagedTri st[kRasterThreads];
@@ -624,14 +624,15 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
                 const uint32_t fl = s.flags;
                 const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31, ry1 = (fl >> 15) & 31;
                 const int area = (rx1 - rx0 + 1) * (ry1 - ry0 + 1);
-                if (!(fl & (1u << 20)) && rx0 <= rx1 && ry0 <= ry1 && area <= a.tune.small_region)
+                if (SmallPath && !(fl & (1u << 20)) && rx0 <= rx1 && ry0 <= ry1 && area <= a.tune.small_region)
                 {
                     // small: this thread rasterizes the triangle's few pixels
                     for (int y = ry0; y <= ry1; y++)
                         for (int x = rx0; x <= rx1; x++)
                         {
                             uint64_t key;
-                            if (fragment_key(s, x, y, less, key))
+                            // a plain read first: most fragments of deep overdraw lose
+                            if (fragment_key(s, x, y, less, key) && key < s_key[y * 16 + x])
                                 atomicMin(&s_key[y * 16 + x], (unsigned long long)key);
                         }
                     s_flags[threadIdx.x] = kEmptyRegion;
@@ -676,10 +677,13 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
         }
 
         // both paths merged; the rank of the winner for k_shade
-        const uint64_t sk = s_key[pix];
-        s_key[pix] = ~0ull;  // ready for the next tile (its first barrier orders this)
-        if (sk < best)
-            best = sk;
+        if (SmallPath)
+        {
+            const uint64_t sk = s_key[pix];
+            s_key[pix] = ~0ull;  // ready for the next tile (its first barrier orders this)
+            if (sk < best)
+                best = sk;
+        }
         const uint32_t low = (uint32_t)best;
         const uint32_t rank = less ? low : ~low;
         const int px = (tileX << 4) + lx, py = (tileY << 4) + ly;
@@ -757,14 +761,20 @@ __global__ void k_back_buffer(const float4* color, uchar4* out, int width, int h
 // -------------------------------------------------------------------------
 
 
+// Raster variants: 0 and 1 carry the triangle-parallel path (no register cap /
+// capped for 5 blocks per SM); 2 is pixel-parallel only, capped for 6.
 static int raster_occupancy(int variant)
 {
-    static int per_sm[2] = { 0, 0 };
+    static int per_sm[3] = { 0, 0, 0 };
     if (!per_sm[variant])
     {
-        const cudaError_t e = variant
-            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[1], k_raster<5>, kRasterThreads, 0)
-            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[0], k_raster<4>, kRasterThreads, 0);
+        cudaError_t e;
+        if (variant == 0)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[0], k_raster<4, true>, kRasterThreads, 0);
+        else if (variant == 1)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[1], k_raster<5, true>, kRasterThreads, 0);
+        else
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[2], k_raster<6, false>, kRasterThreads, 0);
         if (e != cudaSuccess || per_sm[variant] < 1)
             per_sm[variant] = 1;
     }
@@ -773,7 +783,7 @@ static int raster_occupancy(int variant)
 
 static int raster_blocks(int sms, const Tuning& t)
 {
-    const int variant = t.raster_variant ? 1 : 0;
+    const int variant = (t.raster_variant >= 0 && t.raster_variant <= 2) ? t.raster_variant : 1;
     int per = raster_occupancy(variant);
     if (t.raster_blocks_per_sm > 0 && t.raster_blocks_per_sm < per)
         per = t.raster_blocks_per_sm;
@@ -784,6 +794,7 @@ void prepare_kernels()
 {
     raster_occupancy(0);
     raster_occupancy(1);
+    raster_occupancy(2);
 }
 
 Tuning default_tuning()
@@ -826,10 +837,12 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
     k_bin<1><<<bin_blocks, 256, 0, s>>>(a);
     k_bin_big<1><<<sms * 4, 256, 0, s>>>(a);
     mark(5);
-    if (a.tune.raster_variant)
-        k_raster<5><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
+    if (a.tune.raster_variant == 2)
+        k_raster<6, false><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
+    else if (a.tune.raster_variant == 1)
+        k_raster<5, true><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
     else
-        k_raster<4><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
+        k_raster<4, true><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
     mark(6);
     if (a.total_pixels)
         k_shade<<<(unsigned)((a.total_pixels + 255) / 256), 256, 0, s>>>(a);
