@@ -146,7 +146,8 @@ struct edxr_renderer
     Shading shading;
     Camera cam;
 
-    DevBuf frames, clip, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, bins, big_list, counters, status;
+    DevBuf frames, clip, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, bins, bin_tmp, big_list, counters,
+        status;
     DevBuf color, depth, tri_id, back8, diff_scratch, tri_first;
     uint64_t bin_capacity = 0, rtri_cap = 0, poly_cap = 0, big_cap = 0;
     uint64_t debug_cap = 0;  // EDXR_DEBUG_CAPACITY: tiny starting capacities (tests)
@@ -385,6 +386,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     EDXR_CUDA(r->tile_offset.ensure(4 * (tiles + 1)));
     EDXR_CUDA(r->tile_cursor.ensure(4 * (tiles + 1 + nscan + 1)));
     EDXR_CUDA(r->bins.ensure(4 * r->bin_capacity));
+    EDXR_CUDA(r->bin_tmp.ensure(8 * r->bin_capacity));
     EDXR_CUDA(r->big_list.ensure(4 * r->big_cap));
     EDXR_CUDA(r->counters.ensure(4 * 8));
     EDXR_CUDA(r->status.ensure(sizeof(DeviceStatus)));
@@ -412,6 +414,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.tile_offset = r->tile_offset.as<uint32_t>();
     a.tile_cursor = r->tile_cursor.as<uint32_t>();
     a.bins = r->bins.as<uint32_t>();
+    a.bin_tmp = r->bin_tmp.as<uint2>();
     a.bin_capacity = r->bin_capacity;
     a.big_list = r->big_list.as<uint32_t>();
     a.big_capacity = (uint32_t)r->big_cap;
@@ -505,7 +508,9 @@ edxr_status sync_pass(edxr_renderer* r)
             // raster-triangle overflow the count is not final, so retry as well
             r->bin_capacity = st.bins_needed + st.bins_needed / 4 + 1024;
             EDXR_CUDA(r->bins.ensure(4 * r->bin_capacity));
+            EDXR_CUDA(r->bin_tmp.ensure(8 * r->bin_capacity));
             a.bins = r->bins.as<uint32_t>();
+            a.bin_tmp = r->bin_tmp.as<uint2>();
             a.bin_capacity = r->bin_capacity;
         }
         r->rerenders++;
@@ -587,7 +592,7 @@ edxr_status edxr_destroy(edxr_renderer* r)
     if (r->graph)
         cudaGraphExecDestroy(r->graph);
     DevBuf* bufs[] = { &r->frames, &r->clip, &r->rtris, &r->polys, &r->clip_list, &r->tile_count, &r->tile_offset,
-                       &r->tile_cursor, &r->bins, &r->big_list, &r->counters, &r->status, &r->color,
+                       &r->tile_cursor, &r->bins, &r->bin_tmp, &r->big_list, &r->counters, &r->status, &r->color,
                        &r->depth, &r->tri_id, &r->back8, &r->diff_scratch, &r->tri_first };
     for (DevBuf* b : bufs)
         b->release();

@@ -118,10 +118,12 @@ struct PassArgs
     uint32_t* tile_offset;   // total_tiles + 1 (exclusive scan of padded counts)
     uint32_t* tile_cursor;   // total_tiles
     uint32_t* bins;
+    uint2* bin_tmp;          // decided (tile, entry) pairs before the scatter, bin_capacity of them
     uint64_t bin_capacity;
     uint32_t* big_list;      // raster triangles with many tiles, binned by whole blocks
     uint32_t big_capacity;
-    uint32_t* counters;      // [0] raster tris, [1] polys, [2] big tris, [3] raster work queue, [4] clip list
+    uint32_t* counters;      // [0] raster tris, [1] polys, [2] big tris, [3] raster work queue, [4] clip list,
+                             // [5] decided bin entries
     DeviceStatus* status;
     uint32_t* tri_first;     // per flattened input triangle: its first raster triangle (or kNoTriangle)
     float4* color;

@@ -248,6 +248,7 @@ __device__ __forceinline__ void bin_emit(const PassArgs& a, uint32_t ri, uint32_
     const uint32_t act = __activemask();
     const uint32_t tile = d ? tile_in : 0xFFFFFFFFu;
     const uint32_t peers = __match_any_sync(act, tile);
+    const uint32_t hits = __ballot_sync(act, d != 0);
     if (!d)
         return;
     const uint32_t lane = threadIdx.x & 31;
@@ -256,6 +257,15 @@ __device__ __forceinline__ void bin_emit(const PassArgs& a, uint32_t ri, uint32_
     {
         if ((int)lane == leader)
             atomicAdd(&a.tile_count[tile], (uint32_t)__popc(peers));
+        // keep the decided entry in the unsorted list, moved into its bin by
+        // k_bin_move after the scan, so no decision is computed twice
+        const int first = __ffs(hits) - 1;
+        uint32_t base = 0;
+        if ((int)lane == first)
+            base = atomicAdd(&a.counters[5], (uint32_t)__popc(hits));
+        base = __shfl_sync(hits, base, first) + (uint32_t)__popc(hits & ((1u << lane) - 1u));
+        if (base < a.bin_capacity)
+            a.bin_tmp[base] = make_uint2(tile, (ri << 2) | d);
     }
     else
     {
@@ -274,6 +284,33 @@ __device__ __forceinline__ void bin_tile(const PassArgs& a, const FrameDesc& f, 
                                          const Edges& e, const BinGeom& g, int tx, int ty)
 {
     bin_emit<Phase>(a, ri, tile_decision(t, e, g, f, tx, ty), f.tile_base + (uint32_t)(ty * f.tdx + tx));
+}
+
+// Scatter of the decided entries into their bins (after the scan).
+__global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
+{
+    const uint32_t n = *(volatile uint32_t*)&a.counters[5];
+    const uint32_t m = (uint32_t)min((uint64_t)n, a.bin_capacity);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (m + stride - 1) / stride;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t r = 0; r < rounds; r++)
+    {
+        const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const bool valid = i < m;
+        const uint2 e = valid ? a.bin_tmp[i] : make_uint2(0xFFFFFFFFu, 0u);
+        const uint32_t peers = __match_any_sync(0xffffffffu, e.x);
+        if (!valid)
+            continue;
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader)
+            base = atomicAdd(&a.tile_cursor[e.x], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+        const uint64_t pos = (uint64_t)a.tile_offset[e.x] + base;
+        if (pos < a.bin_capacity)
+            a.bins[pos] = e.y;
+    }
 }
 
 template <int Phase>
@@ -472,7 +509,7 @@ struct __align__(16) StagedTri
     int D1, K1, A2, D2;
     int K2;
     uint32_t flags;        // region lx0|lx1<<5|ly0<<10|ly1<<15, accept<<20, bias1<<21, bias2<<22
-    uint32_t rank;         // order + 1
+    uint32_t rank;         // global rank: (frame tri_base * 16 + order) + 1
     uint32_t pad;
     float invDet, z0, z1, z2;
 };
@@ -499,7 +536,8 @@ __device__ __forceinline__ uint32_t zmin_key(const RTri& t)
 
 // Tile-relative edge equations, barycentric numerators and region of one
 // bin entry.
-__device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uint32_t nr, int tileX, int tileY,
+__device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uint32_t nr, uint32_t rank_base,
+                                          int tileX, int tileY,
                                           StagedTri& s, uint32_t& zkey)
 {
     const uint32_t ri = entry >> 2;
@@ -545,7 +583,9 @@ __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uin
               (accept ? (1u << 20) : 0u) | (bias[1] ? (1u << 21) : 0u) | (bias[2] ? (1u << 22) : 0u);
     s.invDet = t.invDet;
     s.z0 = t.z0; s.z1 = t.z1; s.z2 = t.z2;
-    s.rank = t.order + 1u;
+    // submission order within the frame, offset by the frame's first input
+    // triangle so k_shade can find the record without knowing the frame
+    s.rank = rank_base + t.order + 1u;
     zkey = zmin_key(t);
 }
 
@@ -620,7 +660,7 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
             {
                 StagedTri s;
                 uint32_t zk;
-                stage_tri(a, a.bins[start + c + threadIdx.x], nr, tileX, tileY, s, zk);
+                stage_tri(a, a.bins[start + c + threadIdx.x], nr, f.tri_base << 4, tileX, tileY, s, zk);
                 const uint32_t fl = s.flags;
                 const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31, ry1 = (fl >> 15) & 31;
                 const int area = (rx1 - rx0 + 1) * (ry1 - ry0 + 1);
@@ -703,18 +743,17 @@ __global__ void __launch_bounds__(256) k_shade(PassArgs a)
     if (i >= a.total_pixels)
         return;
     const uint32_t rank = a.tri_id[i];
-    const FrameDesc& f = a.frames[frame_of_pixel64(a.frames, a.num_frames, i)];
     const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
     uint32_t ri = kNoTriangle;
     if (rank != 0)
     {
-        const uint32_t order = rank - 1u;
-        const uint32_t gi = f.tri_base + (order >> 4);
+        // rank - 1 = flattened input triangle * 16 + fan index
+        const uint32_t gi = (rank - 1u) >> 4, fan = (rank - 1u) & 15u;
         ri = gi < a.total_tris ? a.tri_first[gi] : kNoTriangle;
         // a clipped triangle's fan pieces are contiguous, in fan order
-        for (int s = 0; s < kMaxPolygon && ri < nr && a.rtris[ri].order != order; s++)
+        for (int s = 0; s < kMaxPolygon && ri < nr && (a.rtris[ri].order & 15u) != fan; s++)
             ri++;
-        if (ri >= nr || a.rtris[ri].order != order)
+        if (ri >= nr || (a.rtris[ri].order & 15u) != fan)
             ri = kNoTriangle;
     }
     if (ri == kNoTriangle)
@@ -725,6 +764,7 @@ __global__ void __launch_bounds__(256) k_shade(PassArgs a)
         return;
     }
     const RTri t = a.rtris[ri];
+    const FrameDesc& f = a.frames[t.meta >> 12];
     const uint64_t local = i - f.pix_base;
     const int px = (int)(local % (uint32_t)f.width), py = (int)(local / (uint32_t)f.width);
     const Edges e = tri_edges(t);
@@ -834,8 +874,7 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
     k_scan_spine<<<1, 1024, 0, s>>>(block_sums, nscan);
     k_scan_add<<<(a.total_tiles + 255) / 256 + 1, 256, 0, s>>>(a, block_sums, nscan);
     mark(4);
-    k_bin<1><<<bin_blocks, 256, 0, s>>>(a);
-    k_bin_big<1><<<sms * 4, 256, 0, s>>>(a);
+    k_bin_move<<<sms * 8, 256, 0, s>>>(a);
     mark(5);
     if (a.tune.raster_variant == 2)
         k_raster<6, false><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
@@ -852,7 +891,7 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
 
 int kernels_per_pass(const PassArgs& a)
 {
-    return 9 + (a.total_vertices ? 1 : 0) + (a.total_tris ? 2 : 0) + (a.total_pixels ? 1 : 0);
+    return 8 + (a.total_vertices ? 1 : 0) + (a.total_tris ? 2 : 0) + (a.total_pixels ? 1 : 0);
 }
 
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s)

@@ -46,7 +46,7 @@ constexpr uint32_t kMaxTiles = 4608;  // >= ceil(W/16)*ceil(H/16) for W*H <= 2^2
 constexpr uint32_t kRtriCap = kMaxTriangles + kMaxTriangles / 4;
 constexpr uint32_t kPolyCap = 8192;
 constexpr uint32_t kBigCap = kRtriCap;
-constexpr uint32_t kBinCap = 1u << 20;
+constexpr uint32_t kBinCap = 3u << 18;
 
 constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -60,13 +60,14 @@ constexpr size_t kOffCount = align256(kOffClipList + 4 * (size_t)kPolyCap);
 constexpr size_t kOffOffset = align256(kOffCount + 4 * (size_t)(kMaxTiles + 1));
 constexpr size_t kOffCursor = align256(kOffOffset + 4 * (size_t)(kMaxTiles + 1));
 constexpr size_t kOffBins = align256(kOffCursor + 4 * (size_t)(kMaxTiles + 1 + 8));
-constexpr size_t kOffBig = align256(kOffBins + 4 * (size_t)kBinCap);
+constexpr size_t kOffBinTmp = align256(kOffBins + 4 * (size_t)kBinCap);
+constexpr size_t kOffBig = align256(kOffBinTmp + 8 * (size_t)kBinCap);
 constexpr size_t kOffCounters = align256(kOffBig + 4 * (size_t)kBigCap);
 constexpr size_t kOffStatus = align256(kOffCounters + 4 * 8);
 constexpr size_t kOffTriFirst = align256(kOffStatus + sizeof(DeviceStatus));
 constexpr size_t kNoAllocScratchBytes = align256(kOffTriFirst + 4 * (size_t)kMaxTriangles);
 
-// The scratch of edxr_render_noalloc (about 12 MiB per device).  Host code
+// The scratch of edxr_render_noalloc (about 17 MiB per device).  Host code
 // only ever sees a host-side stand-in for this name; its device address comes
 // from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -253,6 +254,7 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
     a.tile_offset = reinterpret_cast<uint32_t*>(base + kOffOffset);
     a.tile_cursor = reinterpret_cast<uint32_t*>(base + kOffCursor);
     a.bins = reinterpret_cast<uint32_t*>(base + kOffBins);
+    a.bin_tmp = reinterpret_cast<uint2*>(base + kOffBinTmp);
     a.bin_capacity = kBinCap;
     a.big_list = reinterpret_cast<uint32_t*>(base + kOffBig);
     a.big_capacity = kBigCap;
