@@ -236,8 +236,11 @@ __global__ void __launch_bounds__(128) k_clip(PassArgs a)
 // -------------------------------------------------------------------------
 // Binning.  Phase 0 counts the non-rejected (triangle, tile) pairs per tile,
 // phase 1 writes entries (raster triangle << 2 | decision).  Triangles the
-// reference treats as small go through a lean per-thread path; the others
-// are binned by one warp each with the full decision of tile_decision.
+// reference treats as small go through a lean per-thread path whose
+// decisions are cheap enough to compute again in phase 1; the others are
+// binned by one warp each with the full decision of tile_decision, counted
+// and appended to an unsorted list at once (phase 2) and moved into their
+// bins by k_bin_move after the scan.
 //
 // bin_emit counts or writes one entry for `tile` (decision d; nothing when
 // d is 0).  Neighbouring triangles of a warp often land in the same tile:
@@ -253,12 +256,13 @@ __device__ __forceinline__ void bin_emit(const PassArgs& a, uint32_t ri, uint32_
         return;
     const uint32_t lane = threadIdx.x & 31;
     const int leader = __ffs(peers) - 1;
-    if (Phase == 0)
+    if (Phase != 1)
     {
         if ((int)lane == leader)
             atomicAdd(&a.tile_count[tile], (uint32_t)__popc(peers));
-        // keep the decided entry in the unsorted list, moved into its bin by
-        // k_bin_move after the scan, so no decision is computed twice
+    }
+    if (Phase == 2)
+    {
         const int first = __ffs(hits) - 1;
         uint32_t base = 0;
         if ((int)lane == first)
@@ -267,7 +271,7 @@ __device__ __forceinline__ void bin_emit(const PassArgs& a, uint32_t ri, uint32_
         if (base < a.bin_capacity)
             a.bin_tmp[base] = make_uint2(tile, (ri << 2) | d);
     }
-    else
+    if (Phase == 1)
     {
         uint32_t base = 0;
         if ((int)lane == leader)
@@ -347,8 +351,8 @@ __global__ void __launch_bounds__(256) k_bin(PassArgs a)
     }
 }
 
-// One warp per triangle of the big list; lanes take candidate tiles.
-template <int Phase>
+// One warp per triangle of the big list; lanes take candidate tiles.  Its
+// entries are counted and appended to the unsorted list in one pass.
 __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
 {
     const uint32_t nb = min(*(volatile uint32_t*)&a.counters[2], a.big_capacity);
@@ -363,7 +367,7 @@ __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
         const Edges e = tri_edges(t);
         const int nx = g.t16x1 - g.t16x0 + 1, ny = g.t16y1 - g.t16y0 + 1;
         for (int j = (int)lane; j < nx * ny; j += 32)
-            bin_tile<Phase>(a, f, ri, t, e, g, g.t16x0 + j % nx, g.t16y0 + j / nx);
+            bin_tile<2>(a, f, ri, t, e, g, g.t16x0 + j % nx, g.t16y0 + j / nx);
     }
 }
 
@@ -868,13 +872,14 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
     mark(2);
     const int bin_blocks = sms * (a.tune.bin_blocks_per_sm > 0 ? a.tune.bin_blocks_per_sm : 8);
     k_bin<0><<<bin_blocks, 256, 0, s>>>(a);
-    k_bin_big<0><<<sms * 4, 256, 0, s>>>(a);
+    k_bin_big<<<sms * 4, 256, 0, s>>>(a);
     mark(3);
     k_scan_blocks<<<nscan, kScanThreads, 0, s>>>(a, block_sums);
     k_scan_spine<<<1, 1024, 0, s>>>(block_sums, nscan);
     k_scan_add<<<(a.total_tiles + 255) / 256 + 1, 256, 0, s>>>(a, block_sums, nscan);
     mark(4);
-    k_bin_move<<<sms * 8, 256, 0, s>>>(a);
+    k_bin<1><<<bin_blocks, 256, 0, s>>>(a);
+    k_bin_move<<<sms * 4, 256, 0, s>>>(a);
     mark(5);
     if (a.tune.raster_variant == 2)
         k_raster<6, false><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
@@ -891,7 +896,7 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
 
 int kernels_per_pass(const PassArgs& a)
 {
-    return 8 + (a.total_vertices ? 1 : 0) + (a.total_tris ? 2 : 0) + (a.total_pixels ? 1 : 0);
+    return 9 + (a.total_vertices ? 1 : 0) + (a.total_tris ? 2 : 0) + (a.total_pixels ? 1 : 0);
 }
 
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s)
