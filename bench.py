@@ -14,10 +14,13 @@ Printed JSON (one line, rank 0):
   value       input triangles per second (Mtris/s), inputs resident in HBM,
               device time of K frames from CUDA events on the renderer's
               stream, L2 flushed (a 512 MiB write) before every frame;
-  e2e         the same metric through the public API with pinned host
-              buffers: mesh upload, render and read-back of colour, depth and
-              triangle ids inside the timed region (wall clock);
-  roofline    HBM roofline of the dominant kernel (k_raster, stage events);
+  e2e         the same metric through the public API as the reference's
+              viewer uses it: RenderMesh on a mesh in pinned host memory
+              (uploaded by the call) and GetBackBuffer (the RGBA8 image read
+              back to the host) every frame, wall clock, with a few
+              renderers on their own streams keeping frames in flight;
+  roofline    HBM roofline of the pixel back end (k_raster + k_shade, stage
+              events);
   cpu_baseline the CPU restatement of the reference pipeline (oracle port)
               on this host's cores, one full frame.
 With --impl reference the CPU implementation of the reference pipeline is
@@ -51,6 +54,7 @@ WORKLOADS = {
                lambda: scenes.stress_scene(1_000_000, 3840, 2160, seed=7)),
 }
 PIXEL_BYTES = 24  # RGBA32F colour + D32F depth + u32 triangle id per pixel
+E2E_RENDERERS = 3  # frames in flight in the end-to-end measurement
 
 
 def mesh_bytes(mesh) -> int:
@@ -387,6 +391,60 @@ def measure_diff(device, steps, warmup):
             "fwd_bwd_over_fwd": ms_fb / ms_f}
 
 
+def measure_e2e(sc, device, steps, warmup, workload, world=1, renderers=E2E_RENDERERS):
+    """End to end through the public interface, as the reference's viewer
+    drives it: every frame is RenderMesh on a mesh in pinned host memory
+    (uploaded by the call) followed by GetBackBuffer (the RGBA8 image read
+    back to the host).  `renderers` renderers, each with its own stream and
+    host thread, keep frames in flight so uploads, kernels and read-backs of
+    different frames overlap; every frame still makes all of its own copies."""
+    import threading
+    import torch
+    from edxraster_gb300 import renderer as R
+
+    W, H = sc.view.width, sc.view.height
+    hmesh = R.HostMesh(sc.mesh, pinned=True)
+    rs = []
+    for _ in range(renderers):
+        r = R.Renderer(device=device, stream=torch.cuda.Stream(device=device))
+        r.Initialize(W, H)
+        R.configure(r, sc.view)
+        apply_tuning(r, workload)
+        rs.append(r)
+
+    def frames(r, n):
+        for _ in range(n):
+            r.RenderMesh(hmesh, synchronize=False)
+            r.GetBackBuffer(copy=False)
+
+    def run(total):
+        share = [total // renderers + (1 if k < total % renderers else 0) for k in range(renderers)]
+        ts = [threading.Thread(target=frames, args=(r, n)) for r, n in zip(rs, share)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+
+    run(max(warmup, renderers))
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    run(steps)
+    torch.cuda.synchronize()
+    elapsed = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda:%d" % device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    for r in rs:
+        r.close()
+    return {"value": world * sc.mesh.nt * steps / elapsed / 1e6, "unit": "Mtris/s",
+            "h2d_bytes_per_step": hmesh.nbytes(), "d2h_bytes_per_step": W * H * 4,
+            "ms_per_step": elapsed * 1e3 / steps, "renderers_in_flight": renderers,
+            "step": "RenderMesh(pinned host mesh) + GetBackBuffer (RGBA8 to host)"}
+
+
 def run_gpu(args, world, rank, local):
     import torch
     from edxraster_gb300 import renderer as R
@@ -460,27 +518,8 @@ def run_gpu(args, world, rank, local):
     achieved = raster_bytes / (raster_ms / 1e3) / 1e9
     frame_achieved = algorithmic_bytes(sc) / (ms_per_step / 1e3) / 1e9
 
-    # ---- end to end through the public API with host buffers -----------
-    hmesh = R.HostMesh(sc.mesh, pinned=True)
-    color = torch.empty((H, W, 4), dtype=torch.float32).pin_memory().numpy()
-    depth = torch.empty((H, W), dtype=torch.float32).pin_memory().numpy()
-    tid = torch.empty((H, W), dtype=torch.int32).pin_memory().numpy()
-    lib = r._lib
-
-    def e2e_step():
-        r.RenderMesh(hmesh, synchronize=False)
-        R._lib.check(lib.edxr_read_outputs(r._h, color.ctypes.data, depth.ctypes.data, tid.ctypes.data))
-
-    for _ in range(args.warmup):
-        e2e_step()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = world * sc.mesh.nt * args.steps / e2e_s / 1e6
     r.close()
+    e2e = measure_e2e(sc, local, args.steps, args.warmup, args.workload, world)
 
     # ---- the other configurations (same GPU, shorter runs) ----------------
     per_config = {}
@@ -516,8 +555,7 @@ def run_gpu(args, world, rank, local):
         "roofline": {"kernel": "k_raster+k_shade", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": raster_bytes, "launch_ms": raster_ms},
-        "e2e": {"value": e2e_value, "unit": "Mtris/s", "h2d_bytes_per_step": hmesh.nbytes(),
-                "d2h_bytes_per_step": W * H * PIXEL_BYTES},
+        "e2e": e2e,
         "gpu_launches": int(stats.kernels_per_pass) * args.steps,
         "tuning": r_tuning,
         "clocks": clock_info,

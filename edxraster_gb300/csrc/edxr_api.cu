@@ -131,7 +131,7 @@ struct Shading
 
 struct MeshStage
 {
-    DevBuf pos, nrm, alb, uv, idx;
+    DevBuf pos, nrm, alb, idx;
 };
 
 }  // namespace
@@ -162,7 +162,8 @@ struct edxr_renderer
     bool pending = false;
     uint32_t last_frames = 0, out_width = 0, out_height = 0;
     uint32_t rerenders = 0;
-    std::vector<uint8_t> back_host;
+    uint8_t* back_host = nullptr;  // pinned, GetBackBuffer's RGBA8 copy
+    size_t back_host_cap = 0;
 
     // CUDA graph of the kernel sequence, replayed while the pass layout is unchanged
     bool use_graphs = true;
@@ -273,7 +274,9 @@ edxr_status stage_mesh(edxr_renderer* r, size_t slot, const edxr_mesh* in, edxr_
     if ((st = copy(s.pos, in->positions, in->position_stride, 12, &out->positions, &out->position_stride))) return st;
     if ((st = copy(s.nrm, in->normals, in->normal_stride, 12, &out->normals, &out->normal_stride))) return st;
     if ((st = copy(s.alb, in->albedo, in->albedo_stride, 12, &out->albedo, &out->albedo_stride))) return st;
-    if ((st = copy(s.uv, in->uvs, in->uv_stride, 8, &out->uvs, &out->uv_stride))) return st;
+    // no kernel samples texture coordinates, so they are not uploaded
+    out->uvs = nullptr;
+    out->uv_stride = 0;
     const size_t ib = 12ull * in->num_triangles;
     EDXR_CUDA(s.idx.ensure(ib > 0 ? ib : 16));
     if (ib)
@@ -598,12 +601,14 @@ edxr_status edxr_destroy(edxr_renderer* r)
         b->release();
     for (auto& s : r->stage)
     {
-        s.pos.release(); s.nrm.release(); s.alb.release(); s.uv.release(); s.idx.release();
+        s.pos.release(); s.nrm.release(); s.alb.release(); s.idx.release();
     }
     if (r->frames_host)
         cudaFreeHost(r->frames_host);
     if (r->status_host)
         cudaFreeHost(r->status_host);
+    if (r->back_host)
+        cudaFreeHost(r->back_host);
     if (r->done)
         cudaEventDestroy(r->done);
     for (int i = 0; i < kStageEvents; i++)
@@ -752,10 +757,18 @@ edxr_status edxr_get_back_buffer(edxr_renderer* r, const uint8_t** rgba8)
     EDXR_CUDA(r->back8.ensure(4 * n));
     EDXR_CUDA(launch_back_buffer(r->color.as<float4>(), r->back8.as<uint8_t>(), (int)r->out_width,
                                  (int)r->out_height, r->stream));
-    r->back_host.resize(4 * n);
-    EDXR_CUDA(cudaMemcpyAsync(r->back_host.data(), r->back8.ptr, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    if (r->back_host_cap < 4 * n)
+    {
+        if (r->back_host)
+            cudaFreeHost(r->back_host);
+        r->back_host = nullptr;
+        r->back_host_cap = 0;
+        EDXR_CUDA(cudaMallocHost((void**)&r->back_host, 4 * n));
+        r->back_host_cap = 4 * n;
+    }
+    EDXR_CUDA(cudaMemcpyAsync(r->back_host, r->back8.ptr, 4 * n, cudaMemcpyDeviceToHost, r->stream));
     EDXR_CUDA(cudaStreamSynchronize(r->stream));
-    *rgba8 = r->back_host.data();
+    *rgba8 = r->back_host;
     return EDXR_OK;
 }
 

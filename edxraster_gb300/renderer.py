@@ -92,7 +92,9 @@ class HostMesh:
         self.nv, self.nt = int(self.positions.shape[0]), int(self.indices.shape[0])
 
     def nbytes(self) -> int:
-        return sum(a.nbytes for a in (self.positions, self.normals, self.albedo, self.uvs, self.indices))
+        """Bytes one render call uploads (texture coordinates are not uploaded:
+        no shader samples them)."""
+        return sum(a.nbytes for a in (self.positions, self.normals, self.albedo, self.indices))
 
     def abi(self) -> _lib.Mesh:
         return _lib.Mesh(self.positions.ctypes.data, 12, self.normals.ctypes.data, 12, self.uvs.ctypes.data, 8,
@@ -208,12 +210,18 @@ class Renderer:
     def Synchronize(self):
         _lib.check(self._lib.edxr_synchronize(self._h))
 
-    def GetBackBuffer(self) -> np.ndarray:
-        """Renderer::GetBackBuffer (Renderer.cpp:360-363): RGBA8, bottom-up rows."""
+    def GetBackBuffer(self, copy: bool = True) -> np.ndarray:
+        """Renderer::GetBackBuffer (Renderer.cpp:360-363): RGBA8, bottom-up rows.
+
+        With copy=False the array is a view of the renderer's pinned host
+        buffer, borrowed like the reference's pointer: valid until the next
+        GetBackBuffer, Resize or close of this renderer.
+        """
         p = ctypes.c_void_p()
         _lib.check(self._lib.edxr_get_back_buffer(self._h, ctypes.byref(p)))
         buf = (ctypes.c_uint8 * (4 * self._width * self._height)).from_address(p.value)
-        return np.frombuffer(buf, np.uint8).reshape(self._height, self._width, 4).copy()
+        img = np.frombuffer(buf, np.uint8).reshape(self._height, self._width, 4)
+        return img.copy() if copy else img
 
     def WriteFrameToFile(self, directory: str = "Frames"):
         """Renderer::WriteFrameToFile (Renderer.cpp:352-358): a BMP of the back buffer."""
