@@ -58,6 +58,16 @@ struct DevBuf
             bytes = need;
         return e;
     }
+    // as ensure, and a new allocation starts zeroed (in stream order)
+    cudaError_t ensure_zeroed(size_t need, cudaStream_t s)
+    {
+        if (need <= bytes)
+            return cudaSuccess;
+        cudaError_t e = ensure(need);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(ptr, 0, need, s);
+        return e;
+    }
     void release()
     {
         if (ptr)
@@ -148,7 +158,7 @@ struct edxr_renderer
 
     DevBuf frames, clip, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, bins, bin_tmp, big_list, counters,
         status;
-    DevBuf color, depth, tri_id, back8, diff_scratch, tri_first;
+    DevBuf color, depth, tri_id, back8, diff_scratch, tri_first, items, keybuf;
     uint64_t bin_capacity = 0, rtri_cap = 0, poly_cap = 0, big_cap = 0;
     uint64_t debug_cap = 0;  // EDXR_DEBUG_CAPACITY: tiny starting capacities (tests)
     std::vector<MeshStage> stage;
@@ -396,6 +406,9 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     EDXR_CUDA(r->color.ensure(16 * std::max<uint64_t>(pixels, 1)));
     EDXR_CUDA(r->depth.ensure(4 * std::max<uint64_t>(pixels, 1)));
     EDXR_CUDA(r->tri_id.ensure(4 * std::max<uint64_t>(pixels, 1)));
+    EDXR_CUDA(r->keybuf.ensure_zeroed(8 * std::max<uint64_t>(pixels, 1), r->stream));
+    const uint64_t icap = item_capacity(tiles, r->bin_capacity);
+    EDXR_CUDA(r->items.ensure(sizeof(uint2) * icap));
 
     EDXR_CUDA(cudaMemcpyAsync(r->frames.ptr, r->frames_host, sizeof(FrameDesc) * n, cudaMemcpyHostToDevice, r->stream));
 
@@ -427,6 +440,9 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.depth = r->depth.as<float>();
     a.tri_id = r->tri_id.as<uint32_t>();
     a.tri_first = r->tri_first.as<uint32_t>();
+    a.items = r->items.as<uint2>();
+    a.item_capacity = icap;
+    a.keybuf = r->keybuf.as<unsigned long long>();
     a.total_pixels = pixels;
     a.num_sms = r->num_sms;
 
@@ -515,6 +531,9 @@ edxr_status sync_pass(edxr_renderer* r)
             a.bins = r->bins.as<uint32_t>();
             a.bin_tmp = r->bin_tmp.as<uint2>();
             a.bin_capacity = r->bin_capacity;
+            a.item_capacity = item_capacity(a.total_tiles, r->bin_capacity);
+            EDXR_CUDA(r->items.ensure(sizeof(uint2) * a.item_capacity));
+            a.items = r->items.as<uint2>();
         }
         r->rerenders++;
         EDXR_CUDA(run_pass(r, a));
@@ -596,7 +615,8 @@ edxr_status edxr_destroy(edxr_renderer* r)
         cudaGraphExecDestroy(r->graph);
     DevBuf* bufs[] = { &r->frames, &r->clip, &r->rtris, &r->polys, &r->clip_list, &r->tile_count, &r->tile_offset,
                        &r->tile_cursor, &r->bins, &r->bin_tmp, &r->big_list, &r->counters, &r->status, &r->color,
-                       &r->depth, &r->tri_id, &r->back8, &r->diff_scratch, &r->tri_first };
+                       &r->depth, &r->tri_id, &r->back8, &r->diff_scratch, &r->tri_first, &r->items,
+                       &r->keybuf };
     for (DevBuf* b : bufs)
         b->release();
     for (auto& s : r->stage)

@@ -302,9 +302,28 @@ __device__ __forceinline__ int step_lane(uint32_t corner, int B, int C, int q)
 }
 
 // Per-triangle binning geometry.
+// True when no edge function of t can wrap around int32 at a sample within
+// 64 pixels of its bounding box: every |B*dx + C*dy| there is at most
+// 2 * (extent + 1024)^2 in 1/16-pixel units.  Such a triangle covers a pixel
+// centre only inside its closed outline, so only centres inside the
+// vertices' bounding box can be covered.
+__device__ __forceinline__ bool wrap_free(const RTri& t)
+{
+    const int minx = min(t.v0x, min(t.v1x, t.v2x)), maxx = max(t.v0x, max(t.v1x, t.v2x));
+    const int miny = min(t.v0y, min(t.v1y, t.v2y)), maxy = max(t.v0y, max(t.v1y, t.v2y));
+    const float wx = (float)maxx - (float)minx + 1024.0f, wy = (float)maxy - (float)miny + 1024.0f;
+    return 2.0f * wx * wy < 1073741824.0f;
+}
+
+// Pixels whose centre (16 * p + 8) lies in the closed interval [lo, hi] of
+// 1/16-pixel coordinates: [ceil((lo - 8) / 16), floor((hi - 8) / 16)].
+__device__ __forceinline__ int centre_lo(int lo) { return (int)(((long long)lo + 7) >> 4); }
+__device__ __forceinline__ int centre_hi(int hi) { return (int)(((long long)hi - 8) >> 4); }
+
 struct BinGeom
 {
     int bbx0, bbx1, bby0, bby1;      // pixel bounding box (v >> 4)
+    int cx0, cx1, cy0, cy1;          // pixels whose centre is inside the vertices' bounding box
     int t32x0, t32x1, t32y0, t32y1;  // reference 32x32 tile range (Renderer.cpp:168-171)
     int t16x0, t16x1, t16y0, t16y1;  // candidate 16x16 tiles
     bool small;                      // Renderer.cpp:173
@@ -317,6 +336,8 @@ __device__ __forceinline__ BinGeom bin_geom(const RTri& t, const FrameDesc& f)
     const int miny = min(t.v0y, min(t.v1y, t.v2y)), maxy = max(t.v0y, max(t.v1y, t.v2y));
     g.bbx0 = minx >> 4; g.bbx1 = maxx >> 4;
     g.bby0 = miny >> 4; g.bby1 = maxy >> 4;
+    g.cx0 = centre_lo(minx); g.cx1 = centre_hi(maxx);
+    g.cy0 = centre_lo(miny); g.cy1 = centre_hi(maxy);
     g.t32x0 = max(0, minx >> 9); g.t32x1 = min(f.tdx32 - 1, maxx >> 9);
     g.t32y0 = max(0, miny >> 9); g.t32y1 = min(f.tdy32 - 1, maxy >> 9);
     g.small = (g.t32x1 - g.t32x0 < 2) && (g.t32y1 - g.t32y0 < 2);

@@ -21,6 +21,12 @@ constexpr uint32_t kDecisionFine = 2;    // pixel edge test inside the bounding 
 
 constexpr uint32_t kUnclipped = 0xFFFFFFFFu;
 constexpr uint32_t kNoTriangle = 0xFFFFFFFFu;
+// Raster work item: up to this many bin entries of one tile.  A tile with
+// more entries is split into several items whose winners are merged in a
+// per-pixel key buffer before the last of them shades the tile.
+constexpr uint32_t kItemEntries = 256;
+// Work items of a pass: one per tile plus one per kItemEntries bin entries.
+constexpr uint64_t item_capacity(uint64_t tiles, uint64_t bin_capacity) { return tiles + bin_capacity / kItemEntries + 1; }
 // 3 + one vertex per clip plane is 9 in exact arithmetic; rounding on nearly
 // collinear vertices can add a few more, so the working polygon has room.
 constexpr int kMaxPolygon = 16;
@@ -116,25 +122,28 @@ struct PassArgs
     uint32_t* clip_list;     // input triangles (flattened) that straddle a clip plane
     uint32_t* tile_count;    // total_tiles + 1
     uint32_t* tile_offset;   // total_tiles + 1 (exclusive scan of padded counts)
-    uint32_t* tile_cursor;   // total_tiles
+    uint32_t* tile_cursor;   // total_tiles; the scatter's cursors, then entries of split tiles not yet rastered
     uint32_t* bins;
     uint2* bin_tmp;          // decided (tile, entry) pairs before the scatter, bin_capacity of them
     uint64_t bin_capacity;
     uint32_t* big_list;      // raster triangles with many tiles, binned by whole blocks
     uint32_t big_capacity;
     uint32_t* counters;      // [0] raster tris, [1] polys, [2] big tris, [3] raster work queue, [4] clip list,
-                             // [5] decided bin entries
+                             // [5] decided bin entries, [6] raster work items
+    uint2* items;            // raster work items (tile, index of its kItemEntries-entry slice)
+    uint64_t item_capacity;
+    unsigned long long* keybuf;  // per pixel: ~(smallest key) of split tiles, 0 between passes
     DeviceStatus* status;
     uint32_t* tri_first;     // per flattened input triangle: its first raster triangle (or kNoTriangle)
     float4* color;
     float* depth;
-    uint32_t* tri_id;        // raster writes the winner's rank (order + 1, 0 = none) here, k_shade the input-triangle id
+    uint32_t* tri_id;        // the winner's input-triangle id (kNoTriangle: background)
     uint64_t total_pixels;   // frames * width * height
     int num_sms;
 };
 
 // Host-side launchers (edxr_kernels.cu).
-constexpr int kStageEvents = 8;  // boundaries of the 7 timed stages
+constexpr int kStageEvents = 7;  // boundaries of the 6 timed stages
 // ev: NULL, or kStageEvents events recorded around the stages.
 cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev = nullptr);
 int kernels_per_pass(const PassArgs& a);

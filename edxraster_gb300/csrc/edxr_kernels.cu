@@ -8,11 +8,10 @@
 //                  and the post-pass, per input triangle        RasterTriangle.h:27-153
 //   k_bin*         (triangle, 16x16 tile) decisions, counted,   Renderer.cpp:161-229
 //                  scanned and scattered into per-tile bins
-//   k_raster       persistent tiles: coverage, depth test and   Renderer.cpp:248-270,
-//                  winner per pixel                             Rasterizer.h:32-415,
-//                                                               FrameBuffer.cpp:54-68
-//   k_shade        deferred shading of the winner; one write    Renderer.cpp:272-350
-//                  of colour, depth and triangle id per pixel
+//   k_raster       persistent work items of tiles: coverage,   Renderer.cpp:248-350,
+//                  depth test and winner per pixel, then the    Rasterizer.h:32-415,
+//                  winner shaded: one write of colour, depth    FrameBuffer.cpp:54-68
+//                  and triangle id per pixel
 #include <cuda_runtime.h>
 
 #include "edxr_device.cuh"
@@ -340,9 +339,11 @@ __global__ void __launch_bounds__(256) k_bin(PassArgs a)
         }
         // The reference rasterizes a small triangle with FineRasterize in every
         // tile of its range (Renderer.cpp:173-180), so the decision is "fine"
-        // exactly where the quad-aligned bounding box meets the screen.
-        const int x0 = max(g.bbx0 & ~1, 0), x1 = min(g.bbx1 | 1, f.width - 1);
-        const int y0 = max(g.bby0 & ~1, 0), y1 = min(g.bby1 | 1, f.height - 1);
+        // where the quad-aligned bounding box meets the screen.  Tiles where
+        // no pixel centre can be covered get no entry.
+        const bool wf = wrap_free(t);
+        const int x0 = max(wf ? g.cx0 : g.bbx0 & ~1, 0), x1 = min(wf ? g.cx1 : g.bbx1 | 1, f.width - 1);
+        const int y0 = max(wf ? g.cy0 : g.bby0 & ~1, 0), y1 = min(wf ? g.cy1 : g.bby1 | 1, f.height - 1);
         if (x0 > x1 || y0 > y1)
             continue;
         for (int ty = y0 >> kTileLog2; ty <= (y1 >> kTileLog2); ty++)
@@ -465,11 +466,37 @@ __global__ void __launch_bounds__(1024) k_scan_spine(uint32_t* block_sums, uint3
         block_sums[nblocks] = run;  // grand total
 }
 
+// Final offsets, and the raster work items: one per tile (an empty tile's
+// item writes its background) plus one per further kItemEntries entries.
 __global__ void k_scan_add(PassArgs a, const uint32_t* block_sums, uint32_t nblocks)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t n = 0;
     if (i < a.total_tiles)
-        a.tile_offset[i] += block_sums[i / kScanBlock];
+    {
+        const uint32_t start = a.tile_offset[i] + block_sums[i / kScanBlock];
+        a.tile_offset[i] = start;
+        uint32_t count = a.tile_count[i];
+        if ((uint64_t)start + count > a.bin_capacity)
+            count = 0;  // overflowed frame: k_raster skips the tile's entries too
+        n = max(1u, (count + kItemEntries - 1) / kItemEntries);
+    }
+    // one atomic per warp for the items of its 32 tiles
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += t;
+    }
+    uint32_t base = 0;
+    if (lane == 31 && incl)
+        base = atomicAdd(&a.counters[6], incl);
+    base = __shfl_sync(0xffffffffu, base, 31) + incl - n;
+    for (uint32_t j = 0; j < n; j++)
+        if (base + j < a.item_capacity)
+            a.items[base + j] = make_uint2(i, j);
     if (i == 0)
     {
         const uint64_t total = block_sums[nblocks];
@@ -491,22 +518,24 @@ __global__ void k_scan_add(PassArgs a, const uint32_t* block_sums, uint32_t nblo
 }
 
 // -------------------------------------------------------------------------
-// Raster: persistent blocks take 16x16 tiles from a queue.  The winner of
-// the reference's sequential depth test at a pixel is the fragment with the
+// Raster: persistent warps take work items from a queue.  An item is one
+// 16x16 tile's slice of at most kItemEntries bin entries; the warp keeps one
+// 64-bit key per pixel of the tile in shared memory.  The winner of the
+// reference's sequential depth test at a pixel is the fragment with the
 // smallest key (depth key << 32 | submission rank term): for LEQUAL the last
 // fragment with the smallest depth wins, for LESS the first.  Keys can be
-// combined in any order, so the bin needs no ordering and two paths can
-// share the work:
-//  * small entries (quad-aligned region of at most tune.small_region pixels) are
-//    rasterized triangle-parallel by the thread that stages them, merging
-//    into a shared-memory key per pixel with a 64-bit atomicMin;
+// combined in any order, so the bin needs no ordering and two paths share
+// the work of each group of 32 entries (one staged per lane):
+//  * small entries (quad-aligned region of at most tune.small_region pixels)
+//    are rasterized triangle-parallel by the lane that staged them, merging
+//    into the key array with a shared 64-bit atomicMin;
 //  * the other entries are staged as tile-relative edge equations and
-//    rasterized pixel-parallel: warp w owns the 8x4 block at
-//    (8*(w&1), 4*(w>>1)), tests 32 staged entries at once (one per lane) for
-//    overlap with its block and against its hierarchical depth bound, and
-//    walks only the entries whose ballot bit is set.
-// The pixel's final key is the minimum of both; its rank (order + 1, 0 when
-// nothing passed) goes to the id buffer for k_shade.
+//    rasterized pixel-parallel by the whole warp over their region.
+// Entries whose depth lower bound is behind every pixel of the tile so far
+// (the tile's hierarchical depth bound) are skipped.  The winners are then
+// shaded by the same warp: directly for a tile of one item; for a tile split
+// into several items, by the item that finishes last, after all of them
+// merged their keys in the per-pixel key buffer.
 struct __align__(16) StagedTri
 {
     int A0, D0, K0, A1;    // e0 = A0*lx + D0*ly + K0 (with bias); l1 = A1*lx + D1*ly + K1 (no bias)
@@ -525,12 +554,9 @@ constexpr uint32_t kEmptyRegion = 16u | (16u << 10);  // lx0 = ly0 = 16 > lx1 = 
 // large enough for int32 edge values to wrap.  Without wraparound the
 // barycentrics of rasterized pixels are within a few ulps of [0, 1], so the
 // computed depth is at least min(z) minus a few ulps of the |z| sum.
-__device__ __forceinline__ uint32_t zmin_key(const RTri& t)
+__device__ __forceinline__ uint32_t zmin_key(const RTri& t, bool wf)
 {
-    const int minx = min(t.v0x, min(t.v1x, t.v2x)), maxx = max(t.v0x, max(t.v1x, t.v2x));
-    const int miny = min(t.v0y, min(t.v1y, t.v2y)), maxy = max(t.v0y, max(t.v1y, t.v2y));
-    const float wx = (float)maxx - (float)minx + 1024.0f, wy = (float)maxy - (float)miny + 1024.0f;
-    if (!(2.0f * wx * wy < 1073741824.0f))
+    if (!wf)
         return 0u;
     const float zmin = fminf(t.z0, fminf(t.z1, t.z2));
     const float margin = 2e-6f * (fabsf(t.z0) + fabsf(t.z1) + fabsf(t.z2)) + 1e-30f;
@@ -572,15 +598,21 @@ __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uin
     // and 2 measured from v2, equal to the unbiased edge values
     s.A1 = A[1]; s.D1 = D[1]; s.K1 = K[1];
     s.A2 = A[2]; s.D2 = D[2]; s.K2 = K[2];
+    const bool wf = wrap_free(t);
     int lx0 = 0, lx1 = 15, ly0 = 0, ly1 = 15;
     if (!accept)
     {
-        const int bbx0 = min(t.v0x, min(t.v1x, t.v2x)) >> 4, bbx1 = max(t.v0x, max(t.v1x, t.v2x)) >> 4;
-        const int bby0 = min(t.v0y, min(t.v1y, t.v2y)) >> 4, bby1 = max(t.v0y, max(t.v1y, t.v2y)) >> 4;
-        lx0 = max(0, (bbx0 & ~1) - (tileX << 4));
-        lx1 = min(15, (bbx1 | 1) - (tileX << 4));
-        ly0 = max(0, (bby0 & ~1) - (tileY << 4));
-        ly1 = min(15, (bby1 | 1) - (tileY << 4));
+        // FineRasterize's quad-aligned bounding box (Rasterizer.h:132-140),
+        // or only the pixels whose centre is in the vertices' bounding box
+        // when no edge function can wrap (no other centre can be covered)
+        const int minx = min(t.v0x, min(t.v1x, t.v2x)), maxx = max(t.v0x, max(t.v1x, t.v2x));
+        const int miny = min(t.v0y, min(t.v1y, t.v2y)), maxy = max(t.v0y, max(t.v1y, t.v2y));
+        const int bbx0 = wf ? centre_lo(minx) : (minx >> 4) & ~1, bbx1 = wf ? centre_hi(maxx) : (maxx >> 4) | 1;
+        const int bby0 = wf ? centre_lo(miny) : (miny >> 4) & ~1, bby1 = wf ? centre_hi(maxy) : (maxy >> 4) | 1;
+        lx0 = max(0, bbx0 - (tileX << 4));
+        lx1 = min(15, bbx1 - (tileX << 4));
+        ly0 = max(0, bby0 - (tileY << 4));
+        ly1 = min(15, bby1 - (tileY << 4));
         if (lx1 < lx0 || ly1 < ly0) { lx0 = 16; lx1 = 0; ly0 = 16; ly1 = 0; }
     }
     s.flags = (uint32_t)lx0 | ((uint32_t)lx1 << 5) | ((uint32_t)ly0 << 10) | ((uint32_t)ly1 << 15) |
@@ -588,9 +620,9 @@ __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uin
     s.invDet = t.invDet;
     s.z0 = t.z0; s.z1 = t.z1; s.z2 = t.z2;
     // submission order within the frame, offset by the frame's first input
-    // triangle so k_shade can find the record without knowing the frame
+    // triangle, so the winner's record is found from the rank alone
     s.rank = rank_base + t.order + 1u;
-    zkey = zmin_key(t);
+    zkey = zmin_key(t, wf);
 }
 
 // Key of the fragment of staged triangle s at tile pixel (lx, ly), or false
@@ -620,157 +652,46 @@ __device__ __forceinline__ bool fragment_key(const StagedTri& s, int lx, int ly,
     return true;
 }
 
-template <int MinBlocks, bool SmallPath>
-__global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a)
+// ceil(65536 / w): ((p * kRecip16[w]) >> 16) == p / w for 0 <= p < 256 and
+// 1 <= w <= 16, the row of pixel p of a region w pixels wide.
+__constant__ uint32_t kRecip16[17] = { 0,    65536, 32768, 21846, 16384, 13108, 10923, 9363, 8192,
+                                       7282, 6554,  5958,  5462,  5042,  4682,  4370,  4096 };
+
+constexpr int kRasterWarps = kRasterThreads / 32;
+
+// Raster triangle of the fragment with submission rank `rank` (0: none), or
+// kNoTriangle.  rank - 1 = flattened input triangle * 16 + fan index; the
+// fan pieces of a clipped triangle are contiguous, in fan order, from
+// tri_first.
+__device__ __forceinline__ uint32_t raster_triangle_of(const PassArgs& a, uint32_t rank, uint32_t nr)
 {
-    __shared__ StagedTri st[kRasterThreads];
-    __shared__ uint32_t s_flags[kRasterThreads];
-    __shared__ uint32_t s_zkey[kRasterThreads];
-    __shared__ unsigned long long s_key[kRasterThreads];
-    __shared__ uint32_t s_tile;
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int bx = (int)(warp & 1u) * 8, by = (int)(warp >> 1) * 4;
-    const int lx = bx + (int)(lane & 7u), ly = by + (int)(lane >> 3);
-    const uint32_t pix = (uint32_t)(ly * 16 + lx);  // this thread's pixel in s_key
-    const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
-    s_key[pix] = ~0ull;
-    for (;;)
-    {
-        if (threadIdx.x == 0)
-            s_tile = atomicAdd(&a.counters[3], 1u);
-        __syncthreads();
-        const uint32_t tile = s_tile;
-        __syncthreads();
-        if (tile >= a.total_tiles)
-            break;
-        const uint32_t fi = find_frame(a.frames, a.num_frames, tile, [](const FrameDesc& f) { return f.tile_base; });
-        const FrameDesc& f = a.frames[fi];
-        const uint32_t lt = tile - f.tile_base;
-        const int tileX = (int)(lt % (uint32_t)f.tdx), tileY = (int)(lt / (uint32_t)f.tdx);
-        const bool less = f.depth_func == 1;
-        uint32_t count = a.tile_count[tile];
-        const uint32_t start = a.tile_offset[tile];
-        if ((uint64_t)start + count > a.bin_capacity)
-            count = 0;  // overflowed frame: rendered again by the host
-
-        // clear depth 1.0 with no triangle: rank term ~0 (LEQUAL) or 0 (LESS)
-        uint64_t best = ((uint64_t)0xBF800000u << 32) | (less ? 0u : 0xFFFFFFFFu);
-        uint32_t wzmax = 0xBF800000u;  // largest depth key held in this warp's registers
-
-        for (uint32_t c = 0; c < count; c += kRasterThreads)
-        {
-            const uint32_t m = min((uint32_t)kRasterThreads, count - c);
-            if (threadIdx.x < m)
-            {
-                StagedTri s;
-                uint32_t zk;
-                stage_tri(a, a.bins[start + c + threadIdx.x], nr, f.tri_base << 4, tileX, tileY, s, zk);
-                const uint32_t fl = s.flags;
-                const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31, ry1 = (fl >> 15) & 31;
-                const int area = (rx1 - rx0 + 1) * (ry1 - ry0 + 1);
-                if (SmallPath && !(fl & (1u << 20)) && rx0 <= rx1 && ry0 <= ry1 && area <= a.tune.small_region)
-                {
-                    // small: this thread rasterizes the triangle's few pixels
-                    for (int y = ry0; y <= ry1; y++)
-                        for (int x = rx0; x <= rx1; x++)
-                        {
-                            uint64_t key;
-                            // a plain read first: most fragments of deep overdraw lose
-                            if (fragment_key(s, x, y, less, key) && key < s_key[y * 16 + x])
-                                atomicMin(&s_key[y * 16 + x], (unsigned long long)key);
-                        }
-                    s_flags[threadIdx.x] = kEmptyRegion;
-                }
-                else
-                {
-                    st[threadIdx.x] = s;
-                    s_flags[threadIdx.x] = fl;
-                    s_zkey[threadIdx.x] = zk;
-                }
-            }
-            __syncthreads();
-            for (uint32_t g = 0; g < m; g += 32)
-            {
-                const uint32_t jl = g + lane;
-                bool hit = false;
-                if (jl < m)
-                {
-                    const uint32_t fl = s_flags[jl];
-                    const int lx0 = fl & 31, lx1 = (fl >> 5) & 31, ly0 = (fl >> 10) & 31, ly1 = (fl >> 15) & 31;
-                    hit = lx0 <= bx + 7 && lx1 >= bx && ly0 <= by + 3 && ly1 >= by && s_zkey[jl] <= wzmax;
-                }
-                uint32_t todo = __ballot_sync(0xffffffffu, hit);
-                if (!todo)
-                    continue;
-                while (todo)
-                {
-                    const uint32_t j = g + (uint32_t)(__ffs(todo) - 1);
-                    todo &= todo - 1u;
-                    const StagedTri& s = st[j];
-                    const uint32_t fl = s.flags;
-                    const int lx0 = fl & 31, lx1 = (fl >> 5) & 31, ly0 = (fl >> 10) & 31, ly1 = (fl >> 15) & 31;
-                    if (lx < lx0 || lx > lx1 || ly < ly0 || ly > ly1)
-                        continue;
-                    uint64_t key;
-                    if (fragment_key(s, lx, ly, less, key) && key < best)
-                        best = key;
-                }
-                wzmax = __reduce_max_sync(0xffffffffu, (uint32_t)(best >> 32));
-            }
-            __syncthreads();
-        }
-
-        // both paths merged; the rank of the winner for k_shade
-        if (SmallPath)
-        {
-            const uint64_t sk = s_key[pix];
-            s_key[pix] = ~0ull;  // ready for the next tile (its first barrier orders this)
-            if (sk < best)
-                best = sk;
-        }
-        const uint32_t low = (uint32_t)best;
-        const uint32_t rank = less ? low : ~low;
-        const int px = (tileX << 4) + lx, py = (tileY << 4) + ly;
-        if (px < f.width && py < f.height)
-            a.tri_id[f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px] = rank;
-    }
+    if (rank == 0)
+        return kNoTriangle;
+    const uint32_t gi = (rank - 1u) >> 4, fan = (rank - 1u) & 15u;
+    uint32_t ri = gi < a.total_tris ? a.tri_first[gi] : kNoTriangle;
+    if (fan == 0)
+        return ri < nr ? ri : kNoTriangle;
+    for (int s = 0; s < kMaxPolygon && ri < nr && (a.rtris[ri].order & 15u) != fan; s++)
+        ri++;
+    return (ri < nr && (a.rtris[ri].order & 15u) == fan) ? ri : kNoTriangle;
 }
 
-// Deferred shading of the winners (Renderer.cpp:272-350 shades every
-// fragment and keeps the last; only the winner is shaded here): one thread
-// per pixel finds the winner's raster triangle from its rank, recomputes its
-// barycentrics and depth exactly (RasterTriangle.h:324-337), interpolates and
-// shades, and writes colour, depth and the input-triangle id once.
-__global__ void __launch_bounds__(256) k_shade(PassArgs a)
+// The one write of a pixel (Renderer::FragmentProcessing / UpdateFrameBuffer,
+// Renderer.cpp:272-350, shade every fragment and keep the last; only the
+// winner is shaded here): its barycentrics and depth are recomputed exactly
+// (RasterTriangle.h:324-337), then interpolated and shaded.  Not inlined, so
+// the shading's registers do not weigh on the raster loop.
+static __device__ __noinline__ void write_pixel(const PassArgs& a, const FrameDesc& f, uint32_t ri, uint64_t pix, int px,
+                                            int py)
 {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.total_pixels)
-        return;
-    const uint32_t rank = a.tri_id[i];
-    const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
-    uint32_t ri = kNoTriangle;
-    if (rank != 0)
-    {
-        // rank - 1 = flattened input triangle * 16 + fan index
-        const uint32_t gi = (rank - 1u) >> 4, fan = (rank - 1u) & 15u;
-        ri = gi < a.total_tris ? a.tri_first[gi] : kNoTriangle;
-        // a clipped triangle's fan pieces are contiguous, in fan order
-        for (int s = 0; s < kMaxPolygon && ri < nr && (a.rtris[ri].order & 15u) != fan; s++)
-            ri++;
-        if (ri >= nr || (a.rtris[ri].order & 15u) != fan)
-            ri = kNoTriangle;
-    }
     if (ri == kNoTriangle)
     {
-        a.color[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        a.depth[i] = 1.0f;
-        a.tri_id[i] = kNoTriangle;
+        a.color[pix] = make_float4(0.f, 0.f, 0.f, 0.f);
+        a.depth[pix] = 1.0f;
+        a.tri_id[pix] = kNoTriangle;
         return;
     }
     const RTri t = a.rtris[ri];
-    const FrameDesc& f = a.frames[t.meta >> 12];
-    const uint64_t local = i - f.pix_base;
-    const int px = (int)(local % (uint32_t)f.width), py = (int)(local / (uint32_t)f.width);
     const Edges e = tri_edges(t);
     const int cx = (px << 4) + 8, cy = (py << 4) + 8;
     const int n1 = wadd(wmul(e.B[1], wsub(cx, t.v2x)), wmul(e.C[1], wsub(cy, t.v2y)));
@@ -780,9 +701,176 @@ __global__ void __launch_bounds__(256) k_shade(PassArgs a)
     const float L2 = fsub(fsub(1.0f, L0), L1);
     const float d = fadd(fadd(fmul(L0, t.z0), fmul(L1, t.z1)), fmul(L2, t.z2));
     const float3 c = shade_fragment(f, t, a.polys, L0, L1);
-    a.color[i] = make_float4(c.x, c.y, c.z, 1.0f);
-    a.depth[i] = d;
-    a.tri_id[i] = t.order >> 4;
+    a.color[pix] = make_float4(c.x, c.y, c.z, 1.0f);
+    a.depth[pix] = d;
+    a.tri_id[pix] = t.order >> 4;
+}
+
+template <int MinBlocks, bool SmallPath>
+__global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a)
+{
+    __shared__ unsigned long long s_key[kRasterWarps][256];
+    __shared__ StagedTri s_tri[kRasterWarps][32];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long* key = s_key[warp];
+    StagedTri* staged = s_tri[warp];
+    const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
+    const uint32_t nitems = (uint32_t)min((uint64_t)*(volatile uint32_t*)&a.counters[6], a.item_capacity);
+    const int small_region = min(a.tune.small_region, 64);
+    for (;;)
+    {
+        uint32_t q = 0;
+        if (lane == 0)
+            q = atomicAdd(&a.counters[3], 1u);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= nitems)
+            break;
+        const uint2 item = a.items[q];
+        const uint32_t tile = item.x;
+        const uint32_t fi = find_frame(a.frames, a.num_frames, tile, [](const FrameDesc& f) { return f.tile_base; });
+        const FrameDesc& f = a.frames[fi];
+        const uint32_t lt = tile - f.tile_base;
+        const int tileX = (int)(lt % (uint32_t)f.tdx), tileY = (int)(lt / (uint32_t)f.tdx);
+        const bool less = f.depth_func == 1;
+        uint32_t count = a.tile_count[tile];
+        const uint32_t start = a.tile_offset[tile];
+        if ((uint64_t)start + count > a.bin_capacity)
+            count = 0;  // overflowed frame: rendered again by the host
+        const uint32_t e0 = start + item.y * kItemEntries;
+        const uint32_t e1 = min(start + count, e0 + kItemEntries);
+
+        // clear depth 1.0 with no triangle: rank term ~0 (LEQUAL) or 0 (LESS)
+        const unsigned long long clear = ((unsigned long long)0xBF800000u << 32) | (less ? 0u : 0xFFFFFFFFu);
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            key[lane + 32 * k] = clear;
+        __syncwarp();
+        uint32_t tzmax = 0xBF800000u;  // largest depth key of the tile's pixels so far
+
+        for (uint32_t c = e0; c < e1; c += 32)
+        {
+            const uint32_t m = min(32u, e1 - c);
+            bool big = false;
+            if (lane < m)
+            {
+                StagedTri s;
+                uint32_t zk;
+                stage_tri(a, a.bins[c + lane], nr, f.tri_base << 4, tileX, tileY, s, zk);
+                const uint32_t fl = s.flags;
+                const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31, ry1 = (fl >> 15) & 31;
+                if (zk <= tzmax && rx0 <= rx1 && ry0 <= ry1)
+                {
+                    if (SmallPath && !(fl & (1u << 20)) && (rx1 - rx0 + 1) * (ry1 - ry0 + 1) <= small_region)
+                    {
+                        // small: this lane rasterizes the triangle's few pixels
+                        for (int y = ry0; y <= ry1; y++)
+                            for (int x = rx0; x <= rx1; x++)
+                            {
+                                uint64_t k;
+                                // a plain read first: most fragments of deep overdraw lose
+                                if (fragment_key(s, x, y, less, k) && k < key[y * 16 + x])
+                                    atomicMin(&key[y * 16 + x], (unsigned long long)k);
+                            }
+                    }
+                    else
+                    {
+                        staged[lane] = s;
+                        big = true;
+                    }
+                }
+            }
+            uint32_t todo = __ballot_sync(0xffffffffu, big);
+            __syncwarp();
+            while (todo)
+            {
+                const int j = __ffs(todo) - 1;
+                todo &= todo - 1u;
+                const StagedTri s = staged[j];
+                const uint32_t fl = s.flags;
+                const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31, ry1 = (fl >> 15) & 31;
+                const int rw = rx1 - rx0 + 1, area = rw * (ry1 - ry0 + 1);
+                const uint32_t inv = kRecip16[rw];
+                // each pixel of the region belongs to one lane for this entry
+                for (int p = (int)lane; p < area; p += 32)
+                {
+                    const int dy = (int)(((uint32_t)p * inv) >> 16);
+                    const int x = rx0 + p - dy * rw, y = ry0 + dy;
+                    uint64_t k;
+                    if (fragment_key(s, x, y, less, k) && k < key[y * 16 + x])
+                        key[y * 16 + x] = k;
+                }
+                __syncwarp();
+            }
+            if (c + 32 < e1)
+            {
+                uint32_t mz = 0;
+#pragma unroll
+                for (int k = 0; k < 8; k++)
+                    mz = max(mz, (uint32_t)(key[lane + 32 * k] >> 32));
+                tzmax = __reduce_max_sync(0xffffffffu, mz);
+            }
+        }
+
+        // A tile split into several items merges its keys in the key buffer;
+        // the item that finishes last (the tile's cursor, equal to its entry
+        // count after the scatter, counted down to zero) shades the tile.
+        bool shade = true;
+        if (count > kItemEntries)
+        {
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+            {
+                const int p = (int)lane + 32 * k;
+                const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
+                const unsigned long long kk = key[p];
+                if (px < f.width && py < f.height && kk < clear)
+                    atomicMax(&a.keybuf[f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px], ~kk);
+            }
+            __threadfence();
+            __syncwarp();
+            uint32_t left = 0;
+            if (lane == 0)
+                left = atomicSub(&a.tile_cursor[tile], e1 - e0) - (e1 - e0);
+            shade = __shfl_sync(0xffffffffu, left, 0) == 0;
+            if (shade)
+            {
+                __threadfence();
+#pragma unroll
+                for (int k = 0; k < 8; k++)
+                {
+                    const int p = (int)lane + 32 * k;
+                    const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
+                    if (px < f.width && py < f.height)
+                    {
+                        // read and leave zero for the next pass
+                        const unsigned long long m = atomicExch(
+                            &a.keybuf[f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px], 0ull);
+                        key[p] = m ? ~m : clear;
+                    }
+                }
+            }
+        }
+        if (shade)
+        {
+            // winners' raster triangles first (independent loads), then shading
+            uint32_t ri[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+            {
+                const uint32_t low = (uint32_t)key[lane + 32 * k];
+                ri[k] = raster_triangle_of(a, less ? low : ~low, nr);
+            }
+#pragma unroll 1
+            for (int k = 0; k < 8; k++)
+            {
+                const int p = (int)lane + 32 * k;
+                const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
+                if (px < f.width && py < f.height)
+                    write_pixel(a, f, ri[k], f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px, px, py);
+            }
+        }
+        __syncwarp();
+    }
 }
 
 // -------------------------------------------------------------------------
@@ -888,15 +976,12 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
     else
         k_raster<4, true><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
     mark(6);
-    if (a.total_pixels)
-        k_shade<<<(unsigned)((a.total_pixels + 255) / 256), 256, 0, s>>>(a);
-    mark(7);
     return cudaGetLastError();
 }
 
 int kernels_per_pass(const PassArgs& a)
 {
-    return 9 + (a.total_vertices ? 1 : 0) + (a.total_tris ? 2 : 0) + (a.total_pixels ? 1 : 0);
+    return 9 + (a.total_vertices ? 1 : 0) + (a.total_tris ? 2 : 0);
 }
 
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s)

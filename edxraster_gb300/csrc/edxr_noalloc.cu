@@ -65,9 +65,12 @@ constexpr size_t kOffBig = align256(kOffBinTmp + 8 * (size_t)kBinCap);
 constexpr size_t kOffCounters = align256(kOffBig + 4 * (size_t)kBigCap);
 constexpr size_t kOffStatus = align256(kOffCounters + 4 * 8);
 constexpr size_t kOffTriFirst = align256(kOffStatus + sizeof(DeviceStatus));
-constexpr size_t kNoAllocScratchBytes = align256(kOffTriFirst + 4 * (size_t)kMaxTriangles);
+constexpr size_t kItemCap = item_capacity(kMaxTiles, kBinCap);
+constexpr size_t kOffItems = align256(kOffTriFirst + 4 * (size_t)kMaxTriangles);
+constexpr size_t kOffKeyBuf = align256(kOffItems + sizeof(uint2) * kItemCap);
+constexpr size_t kNoAllocScratchBytes = align256(kOffKeyBuf + 8 * (size_t)kMaxPixels);
 
-// The scratch of edxr_render_noalloc (about 17 MiB per device).  Host code
+// The scratch of edxr_render_noalloc (about 25 MiB per device).  Host code
 // only ever sees a host-side stand-in for this name; its device address comes
 // from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -264,6 +267,10 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
     a.depth = depth;
     a.tri_id = triangle_id;
     a.tri_first = reinterpret_cast<uint32_t*>(base + kOffTriFirst);
+    a.items = reinterpret_cast<uint2*>(base + kOffItems);
+    a.item_capacity = kItemCap;
+    // zero in the array's initial image, and every pass leaves it zero
+    a.keybuf = reinterpret_cast<unsigned long long*>(base + kOffKeyBuf);
     a.total_pixels = (uint64_t)width * height;
     a.num_sms = sms;
 
