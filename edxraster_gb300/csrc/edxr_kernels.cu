@@ -112,11 +112,17 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, int n)
 // Setup of the triangles that need no clipping (all clip codes zero), one
 // thread per input triangle; triangles that straddle a clip plane are queued
 // for k_clip, triangles outside one plane are dropped (Clipper.h:103-109).
+// Both lists are appended to with one atomic per block: the counters are
+// single addresses every block of the grid contends for.
 __global__ void __launch_bounds__(256) k_setup(PassArgs a)
 {
+    __shared__ uint32_t s_warp[8];
+    __shared__ uint32_t s_base[2];
     const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t fi = 0, tri = 0;
     int nOut = 0;
+    bool straddle = false;
     RTri t;
     if (gi < a.total_tris)
     {
@@ -139,15 +145,50 @@ __global__ void __launch_bounds__(256) k_setup(PassArgs a)
             const uint32_t k0 = clip_code(c0), k1 = clip_code(c1), k2 = clip_code(c2);
             if ((k0 | k1 | k2) == 0)
                 nOut = setup_triangle(f, c0, c1, c2, t) ? 1 : 0;
-            else if (!(k0 & k1 & k2))
-            {
-                const uint32_t q = atomicAdd(&a.counters[4], 1u);
-                if (q < a.poly_capacity)
-                    a.clip_list[q] = gi;
-            }
+            else
+                straddle = !(k0 & k1 & k2);
         }
     }
-    const uint32_t base = warp_append(&a.counters[0], nOut);
+    // block-wide exclusive scan of (raster triangles, queued triangles),
+    // packed in the low and high halves of one word (each at most 256)
+    const uint32_t packed = (uint32_t)nOut | ((straddle ? 1u : 0u) << 16);
+    uint32_t incl = packed;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += v;
+    }
+    if (lane == 31)
+        s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0)
+    {
+        const uint32_t w = lane < 8 ? s_warp[lane] : 0u;
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1)
+        {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= (uint32_t)o) wi += v;
+        }
+        if (lane < 8)
+            s_warp[lane] = wi - w;
+        if (lane == 7)
+        {
+            s_base[0] = (wi & 0xFFFFu) ? atomicAdd(&a.counters[0], wi & 0xFFFFu) : 0u;
+            s_base[1] = (wi >> 16) ? atomicAdd(&a.counters[4], wi >> 16) : 0u;
+        }
+    }
+    __syncthreads();
+    const uint32_t excl = s_warp[warp] + incl - packed;
+    if (straddle)
+    {
+        const uint32_t q = s_base[1] + (excl >> 16);
+        if (q < a.poly_capacity)
+            a.clip_list[q] = gi;
+    }
+    const uint32_t base = s_base[0] + (excl & 0xFFFFu);
     if (gi < a.total_tris)
         a.tri_first[gi] = (nOut && base < a.rtri_capacity) ? base : kNoTriangle;  // k_clip sets clipped ones
     if (nOut == 0)
@@ -203,7 +244,13 @@ __global__ void __launch_bounds__(128) k_clip(PassArgs a)
             continue;
         }
         const FrameDesc& f = a.frames[fi];
-        const uint32_t pi = atomicAdd(&a.counters[1], 1u);
+        // one polygon record per lane with output, one atomic per warp
+        const uint32_t act = __activemask();
+        const int first = __ffs(act) - 1;
+        uint32_t pi = 0;
+        if ((int)(threadIdx.x & 31) == first)
+            pi = atomicAdd(&a.counters[1], (uint32_t)__popc(act));
+        pi = __shfl_sync(act, pi, first) + (uint32_t)__popc(act & ((1u << (threadIdx.x & 31)) - 1u));
         if (pi >= a.poly_capacity)
         {
             atomicOr(&a.status->overflow, 4u);
@@ -326,17 +373,26 @@ __global__ void __launch_bounds__(256) k_bin(PassArgs a)
         const RTri t = a.rtris[ri];
         const FrameDesc& f = a.frames[t.meta >> 12];
         const BinGeom g = bin_geom(t, f);
-        if (!g.small)
+        if (Phase == 0)
         {
             // bounding box over 2x2 reference tiles: binned warp-cooperatively
-            if (Phase == 0)
+            // (the list is appended to with one atomic per warp)
+            const uint32_t act = __activemask();
+            const uint32_t bigs = __ballot_sync(act, !g.small);
+            if (!g.small)
             {
-                const uint32_t b = atomicAdd(&a.counters[2], 1u);
+                const uint32_t lane = threadIdx.x & 31;
+                const int leader = __ffs(bigs) - 1;
+                uint32_t b = 0;
+                if ((int)lane == leader)
+                    b = atomicAdd(&a.counters[2], (uint32_t)__popc(bigs));
+                b = __shfl_sync(bigs, b, leader) + (uint32_t)__popc(bigs & ((1u << lane) - 1u));
                 if (b < a.big_capacity)
                     a.big_list[b] = ri;
             }
-            continue;
         }
+        if (!g.small)
+            continue;
         // The reference rasterizes a small triangle with FineRasterize in every
         // tile of its range (Renderer.cpp:173-180), so the decision is "fine"
         // where the quad-aligned bounding box meets the screen.  Tiles where
