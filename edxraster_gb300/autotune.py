@@ -19,7 +19,7 @@ import os
 DEFAULT_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
 
 GRID = {
-    "small_region": [0, 8, 16, 32, 64],
+    "small_region": [0, 4, 16, 64],
     "raster_variant": [0, 1, 2],
     "bin_blocks_per_sm": [4, 8, 16],
 }

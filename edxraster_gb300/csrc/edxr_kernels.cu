@@ -708,12 +708,15 @@ __device__ __forceinline__ bool fragment_key(const StagedTri& s, int lx, int ly,
     return true;
 }
 
-// ceil(65536 / w): ((p * kRecip16[w]) >> 16) == p / w for 0 <= p < 256 and
-// 1 <= w <= 16, the row of pixel p of a region w pixels wide.
-__constant__ uint32_t kRecip16[17] = { 0,    65536, 32768, 21846, 16384, 13108, 10923, 9363, 8192,
-                                       7282, 6554,  5958,  5462,  5042,  4682,  4370,  4096 };
-
 constexpr int kRasterWarps = kRasterThreads / 32;
+
+// A staged entry padded to 80 bytes: lanes reading different entries hit
+// different shared-memory banks.
+struct __align__(16) StagedSlot
+{
+    StagedTri s;
+    uint4 pad;
+};
 
 // Raster triangle of the fragment with submission rank `rank` (0: none), or
 // kNoTriangle.  rank - 1 = flattened input triangle * 16 + fan index; the
@@ -766,10 +769,16 @@ template <int MinBlocks, bool SmallPath>
 __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a)
 {
     __shared__ unsigned long long s_key[kRasterWarps][256];
-    __shared__ StagedTri s_tri[kRasterWarps][32];
+    __shared__ StagedSlot s_tri[kRasterWarps][32];
+    // ceil(65536 / w): ((p * s_recip[w]) >> 16) == p / w for 0 <= p < 256 and
+    // 1 <= w <= 16, the row of pixel p of a region w pixels wide
+    __shared__ uint32_t s_recip[17];
+    if (threadIdx.x >= 1 && threadIdx.x <= 16)
+        s_recip[threadIdx.x] = (65536u + threadIdx.x - 1u) / threadIdx.x;
+    __syncthreads();
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long* key = s_key[warp];
-    StagedTri* staged = s_tri[warp];
+    StagedSlot* staged = s_tri[warp];
     const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
     const uint32_t nitems = (uint32_t)min((uint64_t)*(volatile uint32_t*)&a.counters[6], a.item_capacity);
     const int small_region = min(a.tune.small_region, 64);
@@ -806,6 +815,7 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
         for (uint32_t c = e0; c < e1; c += 32)
         {
             const uint32_t m = min(32u, e1 - c);
+            int nsmall = 0;
             bool big = false;
             if (lane < m)
             {
@@ -816,36 +826,64 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
                 const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31, ry1 = (fl >> 15) & 31;
                 if (zk <= tzmax && rx0 <= rx1 && ry0 <= ry1)
                 {
-                    if (SmallPath && !(fl & (1u << 20)) && (rx1 - rx0 + 1) * (ry1 - ry0 + 1) <= small_region)
-                    {
-                        // small: this lane rasterizes the triangle's few pixels
-                        for (int y = ry0; y <= ry1; y++)
-                            for (int x = rx0; x <= rx1; x++)
-                            {
-                                uint64_t k;
-                                // a plain read first: most fragments of deep overdraw lose
-                                if (fragment_key(s, x, y, less, k) && k < key[y * 16 + x])
-                                    atomicMin(&key[y * 16 + x], (unsigned long long)k);
-                            }
-                    }
+                    staged[lane].s = s;
+                    const int area = (rx1 - rx0 + 1) * (ry1 - ry0 + 1);
+                    if (SmallPath && !(fl & (1u << 20)) && area <= small_region)
+                        nsmall = area;
                     else
-                    {
-                        staged[lane] = s;
                         big = true;
-                    }
                 }
             }
+            // Small entries: their (entry, pixel) pairs are numbered across
+            // the warp and taken 32 at a time, so lanes do not idle while
+            // one lane walks a larger region.
+            int incl = nsmall;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (uint32_t)o) incl += v;
+            }
+            const int pairs = __shfl_sync(0xffffffffu, incl, 31);
+            __syncwarp();
+            for (int base = 0; base < pairs; base += 32)
+            {
+                const int p = base + (int)lane;
+                // owner: the first lane whose inclusive count exceeds p
+                int j = 0;
+#pragma unroll
+                for (int st = 16; st >= 1; st >>= 1)
+                {
+                    const int v = __shfl_sync(0xffffffffu, incl, j + st - 1);
+                    if (v <= p) j += st;
+                }
+                const int first = __shfl_sync(0xffffffffu, incl - nsmall, j);
+                if (p < pairs)
+                {
+                    const StagedTri s = staged[j].s;
+                    const uint32_t fl = s.flags;
+                    const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31;
+                    const int rw = rx1 - rx0 + 1, local = p - first;
+                    const int dy = (int)(((uint32_t)local * s_recip[rw]) >> 16);
+                    const int x = rx0 + local - dy * rw, y = ry0 + dy;
+                    uint64_t k;
+                    // a plain read first: most fragments of deep overdraw lose
+                    if (fragment_key(s, x, y, less, k) && k < key[y * 16 + x])
+                        atomicMin(&key[y * 16 + x], (unsigned long long)k);
+                }
+            }
+            // Other entries: the whole warp over each region in turn.
             uint32_t todo = __ballot_sync(0xffffffffu, big);
             __syncwarp();
             while (todo)
             {
                 const int j = __ffs(todo) - 1;
                 todo &= todo - 1u;
-                const StagedTri s = staged[j];
+                const StagedTri s = staged[j].s;
                 const uint32_t fl = s.flags;
                 const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31, ry1 = (fl >> 15) & 31;
                 const int rw = rx1 - rx0 + 1, area = rw * (ry1 - ry0 + 1);
-                const uint32_t inv = kRecip16[rw];
+                const uint32_t inv = s_recip[rw];
                 // each pixel of the region belongs to one lane for this entry
                 for (int p = (int)lane; p < area; p += 32)
                 {
