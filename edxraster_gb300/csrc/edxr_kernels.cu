@@ -18,7 +18,9 @@
 
 namespace edxr {
 
-constexpr int kRasterThreads = 256;    // one thread per pixel of a 16x16 tile
+constexpr int kRasterThreads = 256;    // 8 warps, each on its own work items
+constexpr uint32_t kBigChunk = 128;    // unsorted-list slots a k_bin_big warp reserves at a time
+constexpr uint32_t kEmptySlot = 0xFFFFFFFFu;
 constexpr int kScanItems = 4;
 constexpr int kScanThreads = 1024;
 constexpr int kScanBlock = kScanItems * kScanThreads;
@@ -285,7 +287,7 @@ __global__ void __launch_bounds__(128) k_clip(PassArgs a)
 // reference treats as small go through a lean per-thread path whose
 // decisions are cheap enough to compute again in phase 1; the others are
 // binned by one warp each with the full decision of tile_decision, counted
-// and appended to an unsorted list at once (phase 2) and moved into their
+// and kept in an unsorted list at once (k_bin_big) and moved into their
 // bins by k_bin_move after the scan.
 //
 // bin_emit counts or writes one entry for `tile` (decision d; nothing when
@@ -297,27 +299,16 @@ __device__ __forceinline__ void bin_emit(const PassArgs& a, uint32_t ri, uint32_
     const uint32_t act = __activemask();
     const uint32_t tile = d ? tile_in : 0xFFFFFFFFu;
     const uint32_t peers = __match_any_sync(act, tile);
-    const uint32_t hits = __ballot_sync(act, d != 0);
     if (!d)
         return;
     const uint32_t lane = threadIdx.x & 31;
     const int leader = __ffs(peers) - 1;
-    if (Phase != 1)
+    if (Phase == 0)
     {
         if ((int)lane == leader)
             atomicAdd(&a.tile_count[tile], (uint32_t)__popc(peers));
     }
-    if (Phase == 2)
-    {
-        const int first = __ffs(hits) - 1;
-        uint32_t base = 0;
-        if ((int)lane == first)
-            base = atomicAdd(&a.counters[5], (uint32_t)__popc(hits));
-        base = __shfl_sync(hits, base, first) + (uint32_t)__popc(hits & ((1u << lane) - 1u));
-        if (base < a.bin_capacity)
-            a.bin_tmp[base] = make_uint2(tile, (ri << 2) | d);
-    }
-    if (Phase == 1)
+    else
     {
         uint32_t base = 0;
         if ((int)lane == leader)
@@ -329,35 +320,19 @@ __device__ __forceinline__ void bin_emit(const PassArgs& a, uint32_t ri, uint32_
     }
 }
 
-template <int Phase>
-__device__ __forceinline__ void bin_tile(const PassArgs& a, const FrameDesc& f, uint32_t ri, const RTri& t,
-                                         const Edges& e, const BinGeom& g, int tx, int ty)
-{
-    bin_emit<Phase>(a, ri, tile_decision(t, e, g, f, tx, ty), f.tile_base + (uint32_t)(ty * f.tdx + tx));
-}
-
-// Scatter of the decided entries into their bins (after the scan).
+// Scatter of the decided entries of big triangles into their bins (after
+// the scan).  The list holds one triangle's tiles in a row, all different,
+// so each entry takes its own atomic; empty slots are skipped.
 __global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
 {
     const uint32_t n = *(volatile uint32_t*)&a.counters[5];
     const uint32_t m = (uint32_t)min((uint64_t)n, a.bin_capacity);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounds = (m + stride - 1) / stride;
-    const uint32_t lane = threadIdx.x & 31;
-    for (uint32_t r = 0; r < rounds; r++)
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
     {
-        const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        const bool valid = i < m;
-        const uint2 e = valid ? a.bin_tmp[i] : make_uint2(0xFFFFFFFFu, 0u);
-        const uint32_t peers = __match_any_sync(0xffffffffu, e.x);
-        if (!valid)
+        const uint2 e = a.bin_tmp[i];
+        if (e.x == kEmptySlot)
             continue;
-        const int leader = __ffs(peers) - 1;
-        uint32_t base = 0;
-        if ((int)lane == leader)
-            base = atomicAdd(&a.tile_cursor[e.x], (uint32_t)__popc(peers));
-        base = __shfl_sync(peers, base, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-        const uint64_t pos = (uint64_t)a.tile_offset[e.x] + base;
+        const uint64_t pos = (uint64_t)a.tile_offset[e.x] + atomicAdd(&a.tile_cursor[e.x], 1u);
         if (pos < a.bin_capacity)
             a.bins[pos] = e.y;
     }
@@ -408,13 +383,22 @@ __global__ void __launch_bounds__(256) k_bin(PassArgs a)
     }
 }
 
-// One warp per triangle of the big list; lanes take candidate tiles.  Its
-// entries are counted and appended to the unsorted list in one pass.
+// One warp per triangle of the big list; lanes take candidate tiles.  Each
+// entry is counted in its tile and kept in the unsorted list, which the
+// warp fills from slots it reserves kBigChunk at a time (one atomic on the
+// shared counter per chunk instead of one per group of 32 candidates);
+// slots it leaves unused are marked empty.
 __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
 {
     const uint32_t nb = min(*(volatile uint32_t*)&a.counters[2], a.big_capacity);
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    uint32_t cbase = 0, cleft = 0;  // the warp's current chunk
+    auto mark_empty = [&]() {
+        for (uint32_t k = lane; k < cleft; k += 32)
+            if (cbase + k < a.bin_capacity)
+                a.bin_tmp[cbase + k] = make_uint2(kEmptySlot, 0u);
+    };
     for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nb; b += nw)
     {
         const uint32_t ri = a.big_list[b];
@@ -423,9 +407,41 @@ __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
         const BinGeom g = bin_geom(t, f);
         const Edges e = tri_edges(t);
         const int nx = g.t16x1 - g.t16x0 + 1, ny = g.t16y1 - g.t16y0 + 1;
-        for (int j = (int)lane; j < nx * ny; j += 32)
-            bin_tile<2>(a, f, ri, t, e, g, g.t16x0 + j % nx, g.t16y0 + j / nx);
+        for (int j0 = 0; j0 < nx * ny; j0 += 32)
+        {
+            const int j = j0 + (int)lane;
+            uint32_t d = 0, tile = 0;
+            if (j < nx * ny)
+            {
+                const int tx = g.t16x0 + j % nx, ty = g.t16y0 + j / nx;
+                d = tile_decision(t, e, g, f, tx, ty);
+                tile = f.tile_base + (uint32_t)(ty * f.tdx + tx);
+            }
+            const uint32_t hits = __ballot_sync(0xffffffffu, d != 0);
+            const uint32_t h = (uint32_t)__popc(hits);
+            if (h == 0)
+                continue;
+            if (h > cleft)
+            {
+                mark_empty();
+                uint32_t nbase = 0;
+                if (lane == 0)
+                    nbase = atomicAdd(&a.counters[5], kBigChunk);
+                cbase = __shfl_sync(0xffffffffu, nbase, 0);
+                cleft = kBigChunk;
+            }
+            if (d)
+            {
+                atomicAdd(&a.tile_count[tile], 1u);
+                const uint32_t pos = cbase + (uint32_t)__popc(hits & ((1u << lane) - 1u));
+                if (pos < a.bin_capacity)
+                    a.bin_tmp[pos] = make_uint2(tile, (ri << 2) | d);
+            }
+            cbase += h;
+            cleft -= h;
+        }
     }
+    mark_empty();
 }
 
 // -------------------------------------------------------------------------
@@ -557,7 +573,9 @@ __global__ void k_scan_add(PassArgs a, const uint32_t* block_sums, uint32_t nblo
     {
         const uint64_t total = block_sums[nblocks];
         a.tile_offset[a.total_tiles] = (uint32_t)total;
-        a.status->bins_needed = total;
+        // the unsorted list of big-triangle entries shares the capacity
+        const uint64_t needed = max(total, (uint64_t)a.counters[5]);
+        a.status->bins_needed = needed;
         a.status->raster_tris = a.counters[0];
         a.status->clipped_polys = a.counters[1];
         a.status->big_tris = a.counters[2];
@@ -566,7 +584,7 @@ __global__ void k_scan_add(PassArgs a, const uint32_t* block_sums, uint32_t nblo
         if (a.counters[1] > a.poly_capacity || a.counters[4] > a.poly_capacity)
             atomicOr(&a.status->overflow, 4u);
         a.status->clipped_polys = max(a.counters[1], a.counters[4]);
-        if (total > a.bin_capacity)
+        if (needed > a.bin_capacity)
             atomicOr(&a.status->overflow, 1u);
         if (a.counters[2] > a.big_capacity)
             atomicOr(&a.status->overflow, 8u);
