@@ -357,21 +357,17 @@ __device__ __forceinline__ bool fine_region_hits(const BinGeom& g, const FrameDe
     return x0 <= x1 && y0 <= y1;
 }
 
-// The reference's treatment of 16x16 tile (tx, ty) for triangle t: 0 (not
+// The reference's treatment of the four 16x16 quadrants of 32x32 tile
+// (T32x, T32y) for a triangle that is not small: per quadrant 0 (not
 // rasterized), kDecisionAccept (TrivialAcceptTriangle: every pixel is
 // depth-tested) or kDecisionFine (FineRasterize: edge test per pixel inside
-// the quad-aligned bounding box).  Follows the binning of
-// Renderer.cpp:173-227, RasterizeTile (Renderer.cpp:248-270) and
+// the quad-aligned bounding box), 2 bits each at quadrant q = (tx & 1) +
+// 2 * (ty & 1), zero for quadrants off the screen's tile range.  Follows the
+// binning of Renderer.cpp:173-227, RasterizeTile (Renderer.cpp:248-270) and
 // CoarseRasterize (Rasterizer.h:32-111) with their int32 wraparound.
-__device__ __forceinline__ uint32_t tile_decision(const RTri& t, const Edges& e, const BinGeom& g,
-                                                  const FrameDesc& f, int tx, int ty)
+__device__ __forceinline__ uint32_t quad_decisions(const RTri& t, const Edges& e, const BinGeom& g,
+                                                   const FrameDesc& f, int T32x, int T32y)
 {
-    const int T32x = tx >> 1, T32y = ty >> 1;
-    if (T32x < g.t32x0 || T32x > g.t32x1 || T32y < g.t32y0 || T32y > g.t32y1)
-        return 0;
-    if (g.small)
-        return fine_region_hits(g, f, tx, ty) ? kDecisionFine : 0;
-
     const int shift = kRefTileLog2 + 4;
     uint32_t rej[3], acc[3];
 #pragma unroll
@@ -380,7 +376,6 @@ __device__ __forceinline__ uint32_t tile_decision(const RTri& t, const Edges& e,
         rej[k] = (t.meta >> (4 * k)) & 3u;
         acc[k] = (t.meta >> (4 * k + 2)) & 3u;
     }
-    bool accE[3];
 #pragma unroll
     for (int k = 0; k < 3; k++)
     {
@@ -389,6 +384,7 @@ __device__ __forceinline__ uint32_t tile_decision(const RTri& t, const Edges& e,
         if (edge_scalar(e, k, cx, cy) < 0)
             return 0;
     }
+    bool accE[3];
 #pragma unroll
     for (int k = 0; k < 3; k++)
     {
@@ -396,34 +392,61 @@ __device__ __forceinline__ uint32_t tile_decision(const RTri& t, const Edges& e,
         const int cy = (T32y + (int)(acc[k] >> 1)) << shift;
         accE[k] = edge_scalar(e, k, cx, cy) >= 0;
     }
+    // quadrants inside the screen's 16x16 tile range
+    uint32_t on = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+        if (2 * T32x + (q & 1) <= g.t16x1 && 2 * T32y + (q >> 1) <= g.t16y1)
+            on |= 1u << q;
+    uint32_t out = 0;
     if (accE[0] && accE[1] && accE[2])
-        return kDecisionAccept;
-    if (!f.hierarchical)
-        return fine_region_hits(g, f, tx, ty) ? kDecisionFine : 0;
-
-    // CoarseRasterize on the 32x32 tile, quadrant q of this 16x16 tile.
-    const int q = (tx & 1) + 2 * (ty & 1);
-    const int baseX = (T32x << kRefTileLog2) << 4, baseY = (T32y << kRefTileLog2) << 4;
-    const int span = (32 << 4) - 1;
-#pragma unroll
-    for (int k = 0; k < 3; k++)
     {
-        const int re = edge_scalar(e, k, baseX + (int)(rej[k] & 1) * span, baseY + (int)(rej[k] >> 1) * span);
-        if (wadd(re, step_lane(rej[k], e.B[k], e.C[k], q)) < 0)
-            return 0;
-    }
-    bool all = true;
 #pragma unroll
-    for (int k = 0; k < 3; k++)
-    {
-        if (accE[k])
-            continue;  // IntSSE(EDX_INFINITY): this edge always accepts
-        const int ae = edge_scalar(e, k, baseX + (int)(acc[k] & 1) * span, baseY + (int)(acc[k] >> 1) * span);
-        all = all && (wadd(ae, step_lane(acc[k], e.B[k], e.C[k], q)) >= 0);
+        for (int q = 0; q < 4; q++)
+            if (on & (1u << q))
+                out |= kDecisionAccept << (2 * q);
+        return out;
     }
-    if (all)
-        return kDecisionAccept;
-    return fine_region_hits(g, f, tx, ty) ? kDecisionFine : 0;
+    int re[3], ae[3];
+    if (f.hierarchical)
+    {
+        const int baseX = (T32x << kRefTileLog2) << 4, baseY = (T32y << kRefTileLog2) << 4;
+        const int span = (32 << 4) - 1;
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+        {
+            re[k] = edge_scalar(e, k, baseX + (int)(rej[k] & 1) * span, baseY + (int)(rej[k] >> 1) * span);
+            ae[k] = edge_scalar(e, k, baseX + (int)(acc[k] & 1) * span, baseY + (int)(acc[k] >> 1) * span);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+    {
+        if (!(on & (1u << q)))
+            continue;
+        const int tx = 2 * T32x + (q & 1), ty = 2 * T32y + (q >> 1);
+        uint32_t d = kDecisionFine;
+        if (f.hierarchical)
+        {
+            // CoarseRasterize on the 32x32 tile, quadrant q
+            bool rejected = false, all = true;
+#pragma unroll
+            for (int k = 0; k < 3; k++)
+            {
+                rejected = rejected || wadd(re[k], step_lane(rej[k], e.B[k], e.C[k], q)) < 0;
+                // IntSSE(EDX_INFINITY): an edge accepted on the whole tile always accepts
+                all = all && (accE[k] || wadd(ae[k], step_lane(acc[k], e.B[k], e.C[k], q)) >= 0);
+            }
+            if (rejected)
+                d = 0;
+            else if (all)
+                d = kDecisionAccept;
+        }
+        if (d == kDecisionFine && !fine_region_hits(g, f, tx, ty))
+            d = 0;
+        out |= d << (2 * q);
+    }
+    return out;
 }
 
 // Monotone key of a depth value: -0 and +0 share a key, float order is

@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(256) k_bin(PassArgs a)
     }
 }
 
-// One warp per triangle of the big list; lanes take candidate tiles.  Each
+// One warp per triangle of the big list; lanes take 32x32 tiles.  Each
 // entry is counted in its tile and kept in the unsorted list, which the
 // warp fills from slots it reserves kBigChunk at a time (one atomic on the
 // shared counter per chunk instead of one per group of 32 candidates);
@@ -406,19 +406,29 @@ __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
         const FrameDesc& f = a.frames[t.meta >> 12];
         const BinGeom g = bin_geom(t, f);
         const Edges e = tri_edges(t);
-        const int nx = g.t16x1 - g.t16x0 + 1, ny = g.t16y1 - g.t16y0 + 1;
+        // lanes take 32x32 reference tiles and decide their four quadrants
+        const int nx = g.t32x1 - g.t32x0 + 1, ny = g.t32y1 - g.t32y0 + 1;
         for (int j0 = 0; j0 < nx * ny; j0 += 32)
         {
             const int j = j0 + (int)lane;
-            uint32_t d = 0, tile = 0;
+            uint32_t dq = 0;
+            int T32x = 0, T32y = 0;
             if (j < nx * ny)
             {
-                const int tx = g.t16x0 + j % nx, ty = g.t16y0 + j / nx;
-                d = tile_decision(t, e, g, f, tx, ty);
-                tile = f.tile_base + (uint32_t)(ty * f.tdx + tx);
+                T32x = g.t32x0 + j % nx;
+                T32y = g.t32y0 + j / nx;
+                dq = quad_decisions(t, e, g, f, T32x, T32y);
             }
-            const uint32_t hits = __ballot_sync(0xffffffffu, d != 0);
-            const uint32_t h = (uint32_t)__popc(hits);
+            const uint32_t nz = (dq | (dq >> 1)) & 0x55u;
+            const int cnt = __popc(nz);
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (uint32_t)o) incl += v;
+            }
+            const uint32_t h = (uint32_t)__shfl_sync(0xffffffffu, incl, 31);
             if (h == 0)
                 continue;
             if (h > cleft)
@@ -430,12 +440,19 @@ __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
                 cbase = __shfl_sync(0xffffffffu, nbase, 0);
                 cleft = kBigChunk;
             }
-            if (d)
+            uint32_t pos = cbase + (uint32_t)(incl - cnt);
+#pragma unroll
+            for (int q = 0; q < 4; q++)
             {
+                const uint32_t d = (dq >> (2 * q)) & 3u;
+                if (!d)
+                    continue;
+                const int tx = 2 * T32x + (q & 1), ty = 2 * T32y + (q >> 1);
+                const uint32_t tile = f.tile_base + (uint32_t)(ty * f.tdx + tx);
                 atomicAdd(&a.tile_count[tile], 1u);
-                const uint32_t pos = cbase + (uint32_t)__popc(hits & ((1u << lane) - 1u));
                 if (pos < a.bin_capacity)
                     a.bin_tmp[pos] = make_uint2(tile, (ri << 2) | d);
+                pos++;
             }
             cbase += h;
             cleft -= h;
