@@ -129,8 +129,9 @@ struct PassArgs
     uint32_t* big_list;      // raster triangles with many tiles, binned by whole blocks
     uint32_t big_capacity;
     uint32_t* counters;      // [0] raster tris, [1] polys, [2] big tris, [3] raster work queue, [4] clip list,
-                             // [5] decided bin entries, [6] raster work items
-    uint2* items;            // raster work items (tile, index of its kItemEntries-entry slice)
+                             // [5] decided bin entries, [6] heavy raster work items, [7] light ones
+    uint2* items;            // raster work items (tile, index of its kItemEntries-entry slice): heavy ones
+                             // from the front, light ones from the back
     uint64_t item_capacity;
     unsigned long long* keybuf;  // per pixel: ~(smallest key) of split tiles, 0 between passes
     DeviceStatus* status;

@@ -21,6 +21,7 @@ namespace edxr {
 constexpr int kRasterThreads = 256;    // 8 warps, each on its own work items
 constexpr uint32_t kBigChunk = 128;    // unsorted-list slots a k_bin_big warp reserves at a time
 constexpr uint32_t kEmptySlot = 0xFFFFFFFFu;
+constexpr uint32_t kHeavyItem = 64;    // raster items with this many entries are handed out first
 constexpr int kScanItems = 4;
 constexpr int kScanThreads = 1024;
 constexpr int kScanBlock = kScanItems * kScanThreads;
@@ -557,35 +558,53 @@ __global__ void __launch_bounds__(1024) k_scan_spine(uint32_t* block_sums, uint3
 
 // Final offsets, and the raster work items: one per tile (an empty tile's
 // item writes its background) plus one per further kItemEntries entries.
+// Items of at least kHeavyItem entries are listed from the front of the
+// item array, the lighter ones from its back, and the queue hands out the
+// front list first: the heavy work starts early instead of forming the tail.
 __global__ void k_scan_add(PassArgs a, const uint32_t* block_sums, uint32_t nblocks)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t n = 0;
+    uint32_t count = 0, n = 0;
     if (i < a.total_tiles)
     {
         const uint32_t start = a.tile_offset[i] + block_sums[i / kScanBlock];
         a.tile_offset[i] = start;
-        uint32_t count = a.tile_count[i];
+        count = a.tile_count[i];
         if ((uint64_t)start + count > a.bin_capacity)
             count = 0;  // overflowed frame: k_raster skips the tile's entries too
         n = max(1u, (count + kItemEntries - 1) / kItemEntries);
     }
-    // one atomic per warp for the items of its 32 tiles
+    // only the last item of a tile can be light
+    const uint32_t last = count - (n - 1) * kItemEntries;
+    const uint32_t nlight = (i < a.total_tiles && last < kHeavyItem) ? 1u : 0u;
+    const uint32_t nheavy = n - nlight;
+    // one atomic per warp and list for the items of its 32 tiles (heavy
+    // count in the low half, light count in the high half)
     const uint32_t lane = threadIdx.x & 31;
-    uint32_t incl = n;
+    const uint32_t packed = nheavy | (nlight << 16);
+    uint32_t incl = packed;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1)
     {
         const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= (uint32_t)o) incl += t;
     }
-    uint32_t base = 0;
-    if (lane == 31 && incl)
-        base = atomicAdd(&a.counters[6], incl);
-    base = __shfl_sync(0xffffffffu, base, 31) + incl - n;
-    for (uint32_t j = 0; j < n; j++)
-        if (base + j < a.item_capacity)
-            a.items[base + j] = make_uint2(i, j);
+    uint32_t hbase = 0, lbase = 0;
+    if (lane == 31)
+    {
+        if (incl & 0xFFFFu)
+            hbase = atomicAdd(&a.counters[6], incl & 0xFFFFu);
+        if (incl >> 16)
+            lbase = atomicAdd(&a.counters[7], incl >> 16);
+    }
+    const uint32_t excl = incl - packed;
+    hbase = __shfl_sync(0xffffffffu, hbase, 31) + (excl & 0xFFFFu);
+    lbase = __shfl_sync(0xffffffffu, lbase, 31) + (excl >> 16);
+    for (uint32_t j = 0; j < nheavy; j++)
+        if (hbase + j < a.item_capacity)
+            a.items[hbase + j] = make_uint2(i, j);
+    if (nlight && lbase < a.item_capacity)
+        a.items[a.item_capacity - 1 - lbase] = make_uint2(i, n - 1);
     if (i == 0)
     {
         const uint64_t total = block_sums[nblocks];
@@ -815,7 +834,8 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
     unsigned long long* key = s_key[warp];
     StagedSlot* staged = s_tri[warp];
     const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
-    const uint32_t nitems = (uint32_t)min((uint64_t)*(volatile uint32_t*)&a.counters[6], a.item_capacity);
+    const uint32_t nheavy = *(volatile uint32_t*)&a.counters[6];
+    const uint32_t nitems = (uint32_t)min((uint64_t)nheavy + *(volatile uint32_t*)&a.counters[7], a.item_capacity);
     const int small_region = min(a.tune.small_region, 64);
     for (;;)
     {
@@ -825,7 +845,7 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
         q = __shfl_sync(0xffffffffu, q, 0);
         if (q >= nitems)
             break;
-        const uint2 item = a.items[q];
+        const uint2 item = a.items[q < nheavy ? q : (uint32_t)(a.item_capacity - 1 - (q - nheavy))];
         const uint32_t tile = item.x;
         const uint32_t fi = find_frame(a.frames, a.num_frames, tile, [](const FrameDesc& f) { return f.tile_base; });
         const FrameDesc& f = a.frames[fi];
