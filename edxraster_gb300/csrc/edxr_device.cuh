@@ -458,7 +458,14 @@ __device__ __forceinline__ uint32_t depth_key(float d)
 }
 
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
-__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// Shading arithmetic (not part of the bit-exact pipeline): fused
+// multiply-adds, one rounding each.
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ float3 lerp3(float b0, float3 a, float b1, float3 b, float b2, float3 c)
+{
+    return f3(fmaf(b0, a.x, fmaf(b1, b.x, b2 * c.x)), fmaf(b0, a.y, fmaf(b1, b.y, b2 * c.y)),
+              fmaf(b0, a.z, fmaf(b1, b.z, b2 * c.z)));
+}
 __device__ __forceinline__ float3 normalize3(float3 v)
 {
     const float inv = 1.0f / sqrtf(dot3(v, v));
@@ -542,7 +549,7 @@ __device__ __forceinline__ float3 shade_model(const FrameDesc& f, float3 P, floa
     }
     switch (f.ps_kind)
     {
-    case 0: return f3(A.x * diffuse + spec, A.y * diffuse + spec, A.z * diffuse + spec);
+    case 0: return f3(fmaf(A.x, diffuse, spec), fmaf(A.y, diffuse, spec), fmaf(A.z, diffuse, spec));
     case 1: return f3(diffuse + spec, diffuse + spec, diffuse + spec);
     case 2: return f3(A.x * diffuse, A.y * diffuse, A.z * diffuse);
     default: return f3(diffuse, diffuse, diffuse);
@@ -609,15 +616,9 @@ __device__ __forceinline__ float3 shade_fragment(const FrameDesc& f, const RTri&
     b1 = fmul(b1, invB);
     b2 = fsub(fsub(1.0f, b0), b1);
     const ShadeVerts v = shade_verts(f, t, polys);
-    const float3 P = f3(b0 * v.p[0].x + b1 * v.p[1].x + b2 * v.p[2].x,
-                        b0 * v.p[0].y + b1 * v.p[1].y + b2 * v.p[2].y,
-                        b0 * v.p[0].z + b1 * v.p[1].z + b2 * v.p[2].z);
-    const float3 N = f3(b0 * v.n[0].x + b1 * v.n[1].x + b2 * v.n[2].x,
-                        b0 * v.n[0].y + b1 * v.n[1].y + b2 * v.n[2].y,
-                        b0 * v.n[0].z + b1 * v.n[1].z + b2 * v.n[2].z);
-    const float3 A = f3(b0 * v.a[0].x + b1 * v.a[1].x + b2 * v.a[2].x,
-                        b0 * v.a[0].y + b1 * v.a[1].y + b2 * v.a[2].y,
-                        b0 * v.a[0].z + b1 * v.a[1].z + b2 * v.a[2].z);
+    const float3 P = lerp3(b0, v.p[0], b1, v.p[1], b2, v.p[2]);
+    const float3 N = lerp3(b0, v.n[0], b1, v.n[1], b2, v.n[2]);
+    const float3 A = lerp3(b0, v.a[0], b1, v.a[1], b2, v.a[2]);
     return shade_model(f, P, N, A);
 }
 

@@ -794,8 +794,17 @@ __device__ __forceinline__ uint32_t raster_triangle_of(const PassArgs& a, uint32
 // winner is shaded here): its barycentrics and depth are recomputed exactly
 // (RasterTriangle.h:324-337), then interpolated and shaded.  Not inlined, so
 // the shading's registers do not weigh on the raster loop.
-static __device__ __noinline__ void write_pixel(const PassArgs& a, const FrameDesc& f, uint32_t ri, uint64_t pix, int px,
-                                            int py)
+struct PixelOut
+{
+    const RTri* rtris;
+    const ClipPoly* polys;
+    float4* color;
+    float* depth;
+    uint32_t* tri_id;
+};
+
+static __device__ __noinline__ void write_pixel(const PixelOut a, const FrameDesc& f, uint32_t ri, uint64_t pix, int px,
+                                                int py)
 {
     if (ri == kNoTriangle)
     {
@@ -837,6 +846,7 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
     const uint32_t nheavy = *(volatile uint32_t*)&a.counters[6];
     const uint32_t nitems = (uint32_t)min((uint64_t)nheavy + *(volatile uint32_t*)&a.counters[7], a.item_capacity);
     const int small_region = min(a.tune.small_region, 64);
+    const PixelOut out = { a.rtris, a.polys, a.color, a.depth, a.tri_id };
     for (;;)
     {
         uint32_t q = 0;
@@ -1015,7 +1025,7 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
                 const int p = (int)lane + 32 * k;
                 const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
                 if (px < f.width && py < f.height)
-                    write_pixel(a, f, ri[k], f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px, px, py);
+                    write_pixel(out, f, ri[k], f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px, px, py);
             }
         }
         __syncwarp();
