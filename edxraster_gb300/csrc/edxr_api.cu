@@ -156,7 +156,7 @@ struct edxr_renderer
     Shading shading;
     Camera cam;
 
-    DevBuf frames, clip, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, bins, bin_tmp, big_list, counters,
+    DevBuf frames, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, bins, bin_tmp, big_list, counters,
         status;
     DevBuf color, depth, tri_id, back8, diff_scratch, tri_first, items, keybuf;
     uint64_t bin_capacity = 0, rtri_cap = 0, poly_cap = 0, big_cap = 0;
@@ -390,7 +390,6 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     const uint64_t rcap = r->rtri_cap, pcap = r->poly_cap;
     const uint64_t nscan = (tiles + 4095) / 4096;
     EDXR_CUDA(r->frames.ensure(sizeof(FrameDesc) * n));
-    EDXR_CUDA(r->clip.ensure(sizeof(float4) * std::max<uint64_t>(tv, 1)));
     EDXR_CUDA(r->tri_first.ensure(4 * std::max<uint64_t>(tt, 1)));
     EDXR_CUDA(r->rtris.ensure(sizeof(RTri) * rcap));
     EDXR_CUDA(r->polys.ensure(sizeof(ClipPoly) * pcap));
@@ -420,7 +419,6 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.total_vertices = (uint32_t)tv;
     a.total_tris = (uint32_t)tt;
     a.total_tiles = (uint32_t)tiles;
-    a.clip = r->clip.as<float4>();
     a.rtris = r->rtris.as<RTri>();
     a.rtri_capacity = (uint32_t)std::min<uint64_t>(rcap, 0xFFFFFFFFu);
     a.polys = r->polys.as<ClipPoly>();
@@ -613,7 +611,7 @@ edxr_status edxr_destroy(edxr_renderer* r)
         cudaEventSynchronize(r->done);
     if (r->graph)
         cudaGraphExecDestroy(r->graph);
-    DevBuf* bufs[] = { &r->frames, &r->clip, &r->rtris, &r->polys, &r->clip_list, &r->tile_count, &r->tile_offset,
+    DevBuf* bufs[] = { &r->frames, &r->rtris, &r->polys, &r->clip_list, &r->tile_count, &r->tile_offset,
                        &r->tile_cursor, &r->bins, &r->bin_tmp, &r->big_list, &r->counters, &r->status, &r->color,
                        &r->depth, &r->tri_id, &r->back8, &r->diff_scratch, &r->tri_first, &r->items,
                        &r->keybuf };

@@ -114,7 +114,6 @@ struct PassArgs
     uint32_t total_vertices;
     uint32_t total_tris;
     uint32_t total_tiles;
-    float4* clip;            // per (frame, vertex) clip position
     RTri* rtris;
     uint32_t rtri_capacity;
     ClipPoly* polys;
@@ -144,7 +143,7 @@ struct PassArgs
 };
 
 // Host-side launchers (edxr_kernels.cu).
-constexpr int kStageEvents = 7;  // boundaries of the 6 timed stages
+constexpr int kStageEvents = 6;  // boundaries of the 5 timed stages
 // ev: NULL, or kStageEvents events recorded around the stages.
 cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev = nullptr);
 int kernels_per_pass(const PassArgs& a);

@@ -3,10 +3,11 @@
 // One pass renders any number of frames (a frame = one mesh seen by one
 // camera); the plain path is a pass of one frame.  Stages:
 //   k_clear        zero the per-tile counters and work queues
-//   k_vertex       clip = MVP * (p, 1) per (frame, vertex)     Shader.h:40-49
-//   k_setup        clip codes, clipping, fixed-point setup      Clipper.h:71-189,
-//                  and the post-pass, per input triangle        RasterTriangle.h:27-153
-//   k_bin*         (triangle, 16x16 tile) decisions, counted,   Renderer.cpp:161-229
+//   k_setup        clip = MVP * (p, 1), clip codes, fixed-point Shader.h:40-49,
+//   k_clip         setup and the post-pass per input triangle;  Clipper.h:71-189,
+//                  clipping of those that straddle a plane;     RasterTriangle.h:27-153
+//                  the count pass of the binning
+//   k_bin_*, scan  (triangle, 16x16 tile) decisions, counted,   Renderer.cpp:161-229
 //                  scanned and scattered into per-tile bins
 //   k_raster       persistent work items of tiles: coverage,   Renderer.cpp:248-350,
 //                  depth test and winner per pixel, then the    Rasterizer.h:32-415,
@@ -49,17 +50,94 @@ __global__ void k_clear(PassArgs a)
 }
 
 // -------------------------------------------------------------------------
-// Vertex stage: one thread per (frame, vertex).
-__global__ void __launch_bounds__(256) k_vertex(PassArgs a)
+// -------------------------------------------------------------------------
+// Binning.  Phase 0 counts the non-rejected (triangle, tile) pairs per tile,
+// phase 1 writes entries (raster triangle << 2 | decision).  Triangles the
+// reference treats as small go through a lean per-thread path whose
+// decisions are cheap enough to compute again in phase 1: counted by the
+// thread that sets the triangle up (k_setup, k_clip), written by
+// k_bin_scatter after the scan.  The others are binned by one warp each with
+// the full decision of quad_decisions, counted and kept in an unsorted list
+// at once (k_bin_big) and moved into their bins by k_bin_move.
+//
+// bin_emit counts or writes one entry for `tile` (decision d; nothing when
+// d is 0).  Neighbouring triangles of a warp often land in the same tile:
+// lanes with equal tiles share one atomic, issued by the lowest lane.
+template <int Phase>
+__device__ __forceinline__ void bin_emit(const PassArgs& a, uint32_t ri, uint32_t d, uint32_t tile_in)
 {
-    const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gi >= a.total_vertices)
+    const uint32_t act = __activemask();
+    const uint32_t tile = d ? tile_in : 0xFFFFFFFFu;
+    const uint32_t peers = __match_any_sync(act, tile);
+    if (!d)
         return;
-    const uint32_t fi = find_frame(a.frames, a.num_frames, gi, [](const FrameDesc& f) { return f.vtx_base; });
-    const FrameDesc& f = a.frames[fi];
-    const uint32_t v = gi - f.vtx_base;
+    const uint32_t lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    if (Phase == 0)
+    {
+        if ((int)lane == leader)
+            atomicAdd(&a.tile_count[tile], (uint32_t)__popc(peers));
+    }
+    else
+    {
+        uint32_t base = 0;
+        if ((int)lane == leader)
+            base = atomicAdd(&a.tile_cursor[tile], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+        const uint64_t pos = (uint64_t)a.tile_offset[tile] + base;
+        if (pos < a.bin_capacity)
+            a.bins[pos] = (ri << 2) | d;
+    }
+}
+
+// A small triangle's entries.  The reference rasterizes a small triangle
+// with FineRasterize in every tile of its range (Renderer.cpp:173-180), so
+// the decision is "fine" where the quad-aligned bounding box meets the
+// screen.  Tiles where no pixel centre can be covered get no entry.
+template <int Phase>
+__device__ __forceinline__ void bin_small(const PassArgs& a, const FrameDesc& f, uint32_t ri, const RTri& t,
+                                          const BinGeom& g)
+{
+    const bool wf = wrap_free(t);
+    const int x0 = max(wf ? g.cx0 : g.bbx0 & ~1, 0), x1 = min(wf ? g.cx1 : g.bbx1 | 1, f.width - 1);
+    const int y0 = max(wf ? g.cy0 : g.bby0 & ~1, 0), y1 = min(wf ? g.cy1 : g.bby1 | 1, f.height - 1);
+    if (x0 > x1 || y0 > y1)
+        return;
+    for (int ty = y0 >> kTileLog2; ty <= (y1 >> kTileLog2); ty++)
+        for (int tx = x0 >> kTileLog2; tx <= (x1 >> kTileLog2); tx++)
+            bin_emit<Phase>(a, ri, kDecisionFine, f.tile_base + (uint32_t)(ty * f.tdx + tx));
+}
+
+// Count pass of one raster triangle, by the thread that set it up: a small
+// one is counted in its tiles, a big one (bounding box over more than 2x2
+// reference tiles) goes to the list k_bin_big bins warp-cooperatively,
+// appended to with one atomic per warp.
+__device__ __forceinline__ void bin_count(const PassArgs& a, const FrameDesc& f, uint32_t ri, const RTri& t)
+{
+    const BinGeom g = bin_geom(t, f);
+    const uint32_t act = __activemask();
+    const uint32_t bigs = __ballot_sync(act, !g.small);
+    if (!g.small)
+    {
+        const uint32_t lane = threadIdx.x & 31;
+        const int leader = __ffs(bigs) - 1;
+        uint32_t b = 0;
+        if ((int)lane == leader)
+            b = atomicAdd(&a.counters[2], (uint32_t)__popc(bigs));
+        b = __shfl_sync(bigs, b, leader) + (uint32_t)__popc(bigs & ((1u << lane) - 1u));
+        if (b < a.big_capacity)
+            a.big_list[b] = ri;
+        return;
+    }
+    bin_small<0>(a, f, ri, t, g);
+}
+
+// Clip-space position of vertex v: clip = MVP * (p, 1) (DefaultVertexShader,
+// Shader.h:40-49), made where it is used instead of in a pass of its own.
+__device__ __forceinline__ float4 clip_position(const FrameDesc& f, uint32_t v)
+{
     const float* p = reinterpret_cast<const float*>(f.positions + (size_t)v * f.pos_stride);
-    a.clip[gi] = xform_point4(f.mvp, __ldg(p), __ldg(p + 1), __ldg(p + 2));
+    return xform_point4(f.mvp, __ldg(p), __ldg(p + 1), __ldg(p + 2));
 }
 
 // -------------------------------------------------------------------------
@@ -142,9 +220,9 @@ __global__ void __launch_bounds__(256) k_setup(PassArgs a)
         }
         else
         {
-            const float4 c0 = a.clip[f.vtx_base + i0];
-            const float4 c1 = a.clip[f.vtx_base + i1];
-            const float4 c2 = a.clip[f.vtx_base + i2];
+            const float4 c0 = clip_position(f, i0);
+            const float4 c1 = clip_position(f, i1);
+            const float4 c2 = clip_position(f, i2);
             const uint32_t k0 = clip_code(c0), k1 = clip_code(c1), k2 = clip_code(c2);
             if ((k0 | k1 | k2) == 0)
                 nOut = setup_triangle(f, c0, c1, c2, t) ? 1 : 0;
@@ -205,6 +283,7 @@ __global__ void __launch_bounds__(256) k_setup(PassArgs a)
     t.meta |= fi << 12;
     t.poly = kUnclipped;
     a.rtris[base] = t;
+    bin_count(a, a.frames[fi], base, t);
 }
 
 // Clipping of the queued triangles (Clipper.h:107-171): Sutherland-Hodgman,
@@ -227,9 +306,9 @@ __global__ void __launch_bounds__(128) k_clip(PassArgs a)
             fi = find_frame(a.frames, a.num_frames, gi, [](const FrameDesc& f) { return f.tri_base; });
             const FrameDesc& f = a.frames[fi];
             tri = gi - f.tri_base;
-            const float4 c0 = a.clip[f.vtx_base + __ldg(f.indices + 3 * (size_t)tri)];
-            const float4 c1 = a.clip[f.vtx_base + __ldg(f.indices + 3 * (size_t)tri + 1)];
-            const float4 c2 = a.clip[f.vtx_base + __ldg(f.indices + 3 * (size_t)tri + 2)];
+            const float4 c0 = clip_position(f, __ldg(f.indices + 3 * (size_t)tri));
+            const float4 c1 = clip_position(f, __ldg(f.indices + 3 * (size_t)tri + 1));
+            const float4 c2 = clip_position(f, __ldg(f.indices + 3 * (size_t)tri + 2));
             const uint32_t k0 = clip_code(c0), k1 = clip_code(c1), k2 = clip_code(c2);
             clip_triangle(f, c0, c1, c2, (k0 ^ k1) | (k1 ^ k2) | (k2 ^ k0), poly, n, vc);
             for (int k = 2; k < n; k++)
@@ -277,47 +356,10 @@ __global__ void __launch_bounds__(128) k_clip(PassArgs a)
             tk.order = (tri << 4) | (uint32_t)(k - 2);
             tk.meta |= fi << 12;
             tk.poly = (pi << 4) | (uint32_t)k;
-            a.rtris[out++] = tk;
+            a.rtris[out] = tk;
+            bin_count(a, f, out, tk);
+            out++;
         }
-    }
-}
-
-// -------------------------------------------------------------------------
-// Binning.  Phase 0 counts the non-rejected (triangle, tile) pairs per tile,
-// phase 1 writes entries (raster triangle << 2 | decision).  Triangles the
-// reference treats as small go through a lean per-thread path whose
-// decisions are cheap enough to compute again in phase 1; the others are
-// binned by one warp each with the full decision of tile_decision, counted
-// and kept in an unsorted list at once (k_bin_big) and moved into their
-// bins by k_bin_move after the scan.
-//
-// bin_emit counts or writes one entry for `tile` (decision d; nothing when
-// d is 0).  Neighbouring triangles of a warp often land in the same tile:
-// lanes with equal tiles share one atomic, issued by the lowest lane.
-template <int Phase>
-__device__ __forceinline__ void bin_emit(const PassArgs& a, uint32_t ri, uint32_t d, uint32_t tile_in)
-{
-    const uint32_t act = __activemask();
-    const uint32_t tile = d ? tile_in : 0xFFFFFFFFu;
-    const uint32_t peers = __match_any_sync(act, tile);
-    if (!d)
-        return;
-    const uint32_t lane = threadIdx.x & 31;
-    const int leader = __ffs(peers) - 1;
-    if (Phase == 0)
-    {
-        if ((int)lane == leader)
-            atomicAdd(&a.tile_count[tile], (uint32_t)__popc(peers));
-    }
-    else
-    {
-        uint32_t base = 0;
-        if ((int)lane == leader)
-            base = atomicAdd(&a.tile_cursor[tile], (uint32_t)__popc(peers));
-        base = __shfl_sync(peers, base, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-        const uint64_t pos = (uint64_t)a.tile_offset[tile] + base;
-        if (pos < a.bin_capacity)
-            a.bins[pos] = (ri << 2) | d;
     }
 }
 
@@ -339,8 +381,8 @@ __global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
     }
 }
 
-template <int Phase>
-__global__ void __launch_bounds__(256) k_bin(PassArgs a)
+// Scatter pass of the small triangles (after the scan).
+__global__ void __launch_bounds__(256) k_bin_scatter(PassArgs a)
 {
     const uint32_t n = *(volatile uint32_t*)&a.counters[0];
     const uint32_t nr = min(n, a.rtri_capacity);
@@ -349,38 +391,8 @@ __global__ void __launch_bounds__(256) k_bin(PassArgs a)
         const RTri t = a.rtris[ri];
         const FrameDesc& f = a.frames[t.meta >> 12];
         const BinGeom g = bin_geom(t, f);
-        if (Phase == 0)
-        {
-            // bounding box over 2x2 reference tiles: binned warp-cooperatively
-            // (the list is appended to with one atomic per warp)
-            const uint32_t act = __activemask();
-            const uint32_t bigs = __ballot_sync(act, !g.small);
-            if (!g.small)
-            {
-                const uint32_t lane = threadIdx.x & 31;
-                const int leader = __ffs(bigs) - 1;
-                uint32_t b = 0;
-                if ((int)lane == leader)
-                    b = atomicAdd(&a.counters[2], (uint32_t)__popc(bigs));
-                b = __shfl_sync(bigs, b, leader) + (uint32_t)__popc(bigs & ((1u << lane) - 1u));
-                if (b < a.big_capacity)
-                    a.big_list[b] = ri;
-            }
-        }
-        if (!g.small)
-            continue;
-        // The reference rasterizes a small triangle with FineRasterize in every
-        // tile of its range (Renderer.cpp:173-180), so the decision is "fine"
-        // where the quad-aligned bounding box meets the screen.  Tiles where
-        // no pixel centre can be covered get no entry.
-        const bool wf = wrap_free(t);
-        const int x0 = max(wf ? g.cx0 : g.bbx0 & ~1, 0), x1 = min(wf ? g.cx1 : g.bbx1 | 1, f.width - 1);
-        const int y0 = max(wf ? g.cy0 : g.bby0 & ~1, 0), y1 = min(wf ? g.cy1 : g.bby1 | 1, f.height - 1);
-        if (x0 > x1 || y0 > y1)
-            continue;
-        for (int ty = y0 >> kTileLog2; ty <= (y1 >> kTileLog2); ty++)
-            for (int tx = x0 >> kTileLog2; tx <= (x1 >> kTileLog2); tx++)
-                bin_emit<Phase>(a, ri, kDecisionFine, f.tile_base + (uint32_t)(ty * f.tdx + tx));
+        if (g.small)
+            bin_small<1>(a, f, ri, t, g);
     }
 }
 
@@ -1108,39 +1120,35 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
     };
     mark(0);
     k_clear<<<(a.total_tiles + 1 + 255) / 256 + 1, 256, 0, s>>>(a);
-    if (a.total_vertices)
-        k_vertex<<<(a.total_vertices + 255) / 256, 256, 0, s>>>(a);
     mark(1);
     if (a.total_tris)
     {
         k_setup<<<(a.total_tris + 255) / 256, 256, 0, s>>>(a);
         k_clip<<<sms * 4, 128, 0, s>>>(a);
     }
-    mark(2);
-    const int bin_blocks = sms * (a.tune.bin_blocks_per_sm > 0 ? a.tune.bin_blocks_per_sm : 8);
-    k_bin<0><<<bin_blocks, 256, 0, s>>>(a);
     k_bin_big<<<sms * 4, 256, 0, s>>>(a);
-    mark(3);
+    mark(2);
     k_scan_blocks<<<nscan, kScanThreads, 0, s>>>(a, block_sums);
     k_scan_spine<<<1, 1024, 0, s>>>(block_sums, nscan);
     k_scan_add<<<(a.total_tiles + 255) / 256 + 1, 256, 0, s>>>(a, block_sums, nscan);
-    mark(4);
-    k_bin<1><<<bin_blocks, 256, 0, s>>>(a);
+    mark(3);
+    const int bin_blocks = sms * (a.tune.bin_blocks_per_sm > 0 ? a.tune.bin_blocks_per_sm : 8);
+    k_bin_scatter<<<bin_blocks, 256, 0, s>>>(a);
     k_bin_move<<<sms * 4, 256, 0, s>>>(a);
-    mark(5);
+    mark(4);
     if (a.tune.raster_variant == 2)
         k_raster<6, false><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
     else if (a.tune.raster_variant == 1)
         k_raster<5, true><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
     else
         k_raster<4, true><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
-    mark(6);
+    mark(5);
     return cudaGetLastError();
 }
 
 int kernels_per_pass(const PassArgs& a)
 {
-    return 9 + (a.total_vertices ? 1 : 0) + (a.total_tris ? 2 : 0);
+    return 8 + (a.total_tris ? 2 : 0);
 }
 
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s)

@@ -52,8 +52,7 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // byte offsets of the sub-buffers inside the array
 constexpr size_t kOffFrame = 0;
-constexpr size_t kOffClip = align256(kOffFrame + sizeof(FrameDesc));
-constexpr size_t kOffRtri = align256(kOffClip + sizeof(float4) * kMaxVertices);
+constexpr size_t kOffRtri = align256(kOffFrame + sizeof(FrameDesc));
 constexpr size_t kOffPoly = align256(kOffRtri + sizeof(RTri) * (size_t)kRtriCap);
 constexpr size_t kOffClipList = align256(kOffPoly + sizeof(ClipPoly) * (size_t)kPolyCap);
 constexpr size_t kOffCount = align256(kOffClipList + 4 * (size_t)kPolyCap);
@@ -70,7 +69,7 @@ constexpr size_t kOffItems = align256(kOffTriFirst + 4 * (size_t)kMaxTriangles);
 constexpr size_t kOffKeyBuf = align256(kOffItems + sizeof(uint2) * kItemCap);
 constexpr size_t kNoAllocScratchBytes = align256(kOffKeyBuf + 8 * (size_t)kMaxPixels);
 
-// The scratch of edxr_render_noalloc (about 25 MiB per device).  Host code
+// The scratch of edxr_render_noalloc (about 24 MiB per device).  Host code
 // only ever sees a host-side stand-in for this name; its device address comes
 // from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -247,7 +246,6 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
     a.total_vertices = f.nv;
     a.total_tris = f.nt;
     a.total_tiles = tiles;
-    a.clip = reinterpret_cast<float4*>(base + kOffClip);
     a.rtris = reinterpret_cast<RTri*>(base + kOffRtri);
     a.rtri_capacity = kRtriCap;
     a.polys = reinterpret_cast<ClipPoly*>(base + kOffPoly);

@@ -271,7 +271,7 @@ class Renderer:
         _lib.check(self._lib.edxr_get_tuning(self._h, ctypes.byref(t)))
         return {k: int(getattr(t, k)) for k in self.TUNING_FIELDS}
 
-    STAGES = ("clear+vertex", "clip+setup", "bin count", "bin scan", "bin scatter", "raster+shade")
+    STAGES = ("clear", "setup+bin count", "bin scan", "bin scatter", "raster+shade")
 
     def SetProfiling(self, enable: bool):
         _lib.check(self._lib.edxr_set_profiling(self._h, 1 if enable else 0))

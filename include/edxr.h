@@ -189,8 +189,8 @@ edxr_status edxr_get_stats(edxr_renderer* r, edxr_stats* stats);
  * RealtimeViewer/Main.cpp:77-84).  While enabled, every pass is launched
  * without graph replay and CUDA events are recorded on the renderer's stream
  * around its stages:
- *   0 clear + vertex transform, 1 clip + setup, 2 bin count, 3 bin scan,
- *   4 bin scatter, 5 raster + shade (coverage, depth test, the winner's
+ *   0 clear, 1 vertex transform + clipping + setup + bin count, 2 bin scan,
+ *   3 bin scatter, 4 raster + shade (coverage, depth test, the winner's
  *   shading and the output writes).
  * edxr_get_stage_times synchronizes and writes the last pass's milliseconds
  * per stage into ms[0..*count-1] (capacity given in *count on entry). */
@@ -294,7 +294,7 @@ edxr_status edxr_backward(edxr_renderer* r, const edxr_mesh* mesh, const edxr_sh
  * The caller passes the mesh (device memory), the camera, the state and the
  * shader, and the three output images (device memory, width*height*4 floats,
  * width*height floats, width*height u32).  Every intermediate buffer lives in
- * one fixed file-scope device array (about 25 MiB, held by every GPU that
+ * one fixed file-scope device array (about 24 MiB, held by every GPU that
  * loads the library until exit); nothing is allocated.  Limits: 65536
  * vertices, 65536 triangles, 4096 pixels per side and 2^20 pixels; larger
  * requests fail with EDXR_ERR_INVALID_ARG, and a frame whose bins or clipped
