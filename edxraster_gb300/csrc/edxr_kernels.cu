@@ -51,85 +51,81 @@ __global__ void k_clear(PassArgs a)
 
 // -------------------------------------------------------------------------
 // -------------------------------------------------------------------------
-// Binning.  Phase 0 counts the non-rejected (triangle, tile) pairs per tile,
-// phase 1 writes entries (raster triangle << 2 | decision).  Triangles the
-// reference treats as small go through a lean per-thread path whose
-// decisions are cheap enough to compute again in phase 1: counted by the
-// thread that sets the triangle up (k_setup, k_clip), written by
-// k_bin_scatter after the scan.  The others are binned by one warp each with
-// the full decision of quad_decisions, counted and kept in an unsorted list
-// at once (k_bin_big) and moved into their bins by k_bin_move.
+// Binning.  Every non-rejected (triangle, tile) pair is counted in its tile
+// and kept as (tile, raster triangle << 2 | decision) in an unsorted list;
+// after the scan of the counts, k_bin_move moves the entries into their
+// bins.  Triangles the reference treats as small are binned by the thread
+// that sets them up (k_setup, k_clip); the others by one warp each with the
+// full decision of quad_decisions (k_bin_big).
 //
-// bin_emit counts or writes one entry for `tile` (decision d; nothing when
-// d is 0).  Neighbouring triangles of a warp often land in the same tile:
-// lanes with equal tiles share one atomic, issued by the lowest lane.
-template <int Phase>
-__device__ __forceinline__ void bin_emit(const PassArgs& a, uint32_t ri, uint32_t d, uint32_t tile_in)
+// bin_count_tile counts one entry of `tile`.  Neighbouring triangles of a
+// warp often land in the same tile: lanes with equal tiles share one atomic,
+// issued by the lowest lane.
+__device__ __forceinline__ void bin_count_tile(const PassArgs& a, uint32_t tile)
 {
     const uint32_t act = __activemask();
-    const uint32_t tile = d ? tile_in : 0xFFFFFFFFu;
     const uint32_t peers = __match_any_sync(act, tile);
-    if (!d)
-        return;
-    const uint32_t lane = threadIdx.x & 31;
-    const int leader = __ffs(peers) - 1;
-    if (Phase == 0)
-    {
-        if ((int)lane == leader)
-            atomicAdd(&a.tile_count[tile], (uint32_t)__popc(peers));
-    }
-    else
-    {
-        uint32_t base = 0;
-        if ((int)lane == leader)
-            base = atomicAdd(&a.tile_cursor[tile], (uint32_t)__popc(peers));
-        base = __shfl_sync(peers, base, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-        const uint64_t pos = (uint64_t)a.tile_offset[tile] + base;
-        if (pos < a.bin_capacity)
-            a.bins[pos] = (ri << 2) | d;
-    }
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1)
+        atomicAdd(&a.tile_count[tile], (uint32_t)__popc(peers));
 }
 
 // A small triangle's entries.  The reference rasterizes a small triangle
 // with FineRasterize in every tile of its range (Renderer.cpp:173-180), so
 // the decision is "fine" where the quad-aligned bounding box meets the
 // screen.  Tiles where no pixel centre can be covered get no entry.
-template <int Phase>
-__device__ __forceinline__ void bin_small(const PassArgs& a, const FrameDesc& f, uint32_t ri, const RTri& t,
-                                          const BinGeom& g)
+struct SmallTiles
+{
+    int tx0, tx1, ty0, ty1;
+};
+
+// The tile range of a small triangle's entries and their number.
+__device__ __forceinline__ uint32_t small_tiles(const FrameDesc& f, const RTri& t, const BinGeom& g, SmallTiles& st)
 {
     const bool wf = wrap_free(t);
     const int x0 = max(wf ? g.cx0 : g.bbx0 & ~1, 0), x1 = min(wf ? g.cx1 : g.bbx1 | 1, f.width - 1);
     const int y0 = max(wf ? g.cy0 : g.bby0 & ~1, 0), y1 = min(wf ? g.cy1 : g.bby1 | 1, f.height - 1);
     if (x0 > x1 || y0 > y1)
-        return;
-    for (int ty = y0 >> kTileLog2; ty <= (y1 >> kTileLog2); ty++)
-        for (int tx = x0 >> kTileLog2; tx <= (x1 >> kTileLog2); tx++)
-            bin_emit<Phase>(a, ri, kDecisionFine, f.tile_base + (uint32_t)(ty * f.tdx + tx));
+        return 0;
+    st.tx0 = x0 >> kTileLog2;
+    st.tx1 = x1 >> kTileLog2;
+    st.ty0 = y0 >> kTileLog2;
+    st.ty1 = y1 >> kTileLog2;
+    return (uint32_t)((st.tx1 - st.tx0 + 1) * (st.ty1 - st.ty0 + 1));
 }
 
-// Count pass of one raster triangle, by the thread that set it up: a small
-// one is counted in its tiles, a big one (bounding box over more than 2x2
-// reference tiles) goes to the list k_bin_big bins warp-cooperatively,
-// appended to with one atomic per warp.
-__device__ __forceinline__ void bin_count(const PassArgs& a, const FrameDesc& f, uint32_t ri, const RTri& t)
+// Counts a small triangle's entries in their tiles and keeps them in the
+// unsorted list from `slot` on (the caller reserved their number).
+__device__ __forceinline__ void bin_small(const PassArgs& a, const FrameDesc& f, uint32_t ri, const SmallTiles& st,
+                                          uint32_t slot)
 {
-    const BinGeom g = bin_geom(t, f);
+    for (int ty = st.ty0; ty <= st.ty1; ty++)
+        for (int tx = st.tx0; tx <= st.tx1; tx++)
+        {
+            const uint32_t tile = f.tile_base + (uint32_t)(ty * f.tdx + tx);
+            bin_count_tile(a, tile);
+            if (slot < a.bin_capacity)
+                a.bin_tmp[slot] = make_uint2(tile, (ri << 2) | kDecisionFine);
+            slot++;
+        }
+}
+
+// A big triangle (bounding box over more than 2x2 reference tiles) goes to
+// the list k_bin_big bins warp-cooperatively, appended to with one atomic
+// per warp.
+__device__ __forceinline__ void bin_big_append(const PassArgs& a, uint32_t ri, bool big)
+{
     const uint32_t act = __activemask();
-    const uint32_t bigs = __ballot_sync(act, !g.small);
-    if (!g.small)
-    {
-        const uint32_t lane = threadIdx.x & 31;
-        const int leader = __ffs(bigs) - 1;
-        uint32_t b = 0;
-        if ((int)lane == leader)
-            b = atomicAdd(&a.counters[2], (uint32_t)__popc(bigs));
-        b = __shfl_sync(bigs, b, leader) + (uint32_t)__popc(bigs & ((1u << lane) - 1u));
-        if (b < a.big_capacity)
-            a.big_list[b] = ri;
+    const uint32_t bigs = __ballot_sync(act, big);
+    if (!big)
         return;
-    }
-    bin_small<0>(a, f, ri, t, g);
+    const uint32_t lane = threadIdx.x & 31;
+    const int leader = __ffs(bigs) - 1;
+    uint32_t b = 0;
+    if ((int)lane == leader)
+        b = atomicAdd(&a.counters[2], (uint32_t)__popc(bigs));
+    b = __shfl_sync(bigs, b, leader) + (uint32_t)__popc(bigs & ((1u << lane) - 1u));
+    if (b < a.big_capacity)
+        a.big_list[b] = ri;
 }
 
 // Clip-space position of vertex v: clip = MVP * (p, 1) (DefaultVertexShader,
@@ -193,17 +189,21 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, int n)
 // Setup of the triangles that need no clipping (all clip codes zero), one
 // thread per input triangle; triangles that straddle a clip plane are queued
 // for k_clip, triangles outside one plane are dropped (Clipper.h:103-109).
-// Both lists are appended to with one atomic per block: the counters are
-// single addresses every block of the grid contends for.
+// A small set-up triangle is binned here as well.  The raster-triangle list,
+// the clip queue and the unsorted bin list are appended to with one atomic
+// per block each: the counters are single addresses every block of the grid
+// contends for.
 __global__ void __launch_bounds__(256) k_setup(PassArgs a)
 {
-    __shared__ uint32_t s_warp[8];
-    __shared__ uint32_t s_base[2];
+    __shared__ uint32_t s_warp[8], s_went[8];
+    __shared__ uint32_t s_base[3];
     const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t fi = 0, tri = 0;
     int nOut = 0;
-    bool straddle = false;
+    bool straddle = false, big = false;
+    uint32_t nent = 0;
+    SmallTiles st;
     RTri t;
     if (gi < a.total_tris)
     {
@@ -225,40 +225,67 @@ __global__ void __launch_bounds__(256) k_setup(PassArgs a)
             const float4 c2 = clip_position(f, i2);
             const uint32_t k0 = clip_code(c0), k1 = clip_code(c1), k2 = clip_code(c2);
             if ((k0 | k1 | k2) == 0)
+            {
                 nOut = setup_triangle(f, c0, c1, c2, t) ? 1 : 0;
+                if (nOut)
+                {
+                    const BinGeom g = bin_geom(t, f);
+                    big = !g.small;
+                    if (g.small)
+                        nent = small_tiles(f, t, g, st);
+                }
+            }
             else
                 straddle = !(k0 & k1 & k2);
         }
     }
-    // block-wide exclusive scan of (raster triangles, queued triangles),
-    // packed in the low and high halves of one word (each at most 256)
+    // block-wide exclusive scans of (raster triangles, queued triangles),
+    // packed in the low and high halves of one word (each at most 256), and
+    // of the bin entries
     const uint32_t packed = (uint32_t)nOut | ((straddle ? 1u : 0u) << 16);
-    uint32_t incl = packed;
+    uint32_t incl = packed, eincl = nent;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1)
     {
         const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= (uint32_t)o) incl += v;
+        const uint32_t ve = __shfl_up_sync(0xffffffffu, eincl, o);
+        if (lane >= (uint32_t)o)
+        {
+            incl += v;
+            eincl += ve;
+        }
     }
     if (lane == 31)
+    {
         s_warp[warp] = incl;
+        s_went[warp] = eincl;
+    }
     __syncthreads();
     if (warp == 0)
     {
-        const uint32_t w = lane < 8 ? s_warp[lane] : 0u;
-        uint32_t wi = w;
+        const uint32_t w = lane < 8 ? s_warp[lane] : 0u, we = lane < 8 ? s_went[lane] : 0u;
+        uint32_t wi = w, wei = we;
 #pragma unroll
         for (int o = 1; o < 8; o <<= 1)
         {
             const uint32_t v = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= (uint32_t)o) wi += v;
+            const uint32_t ve = __shfl_up_sync(0xffffffffu, wei, o);
+            if (lane >= (uint32_t)o)
+            {
+                wi += v;
+                wei += ve;
+            }
         }
         if (lane < 8)
+        {
             s_warp[lane] = wi - w;
+            s_went[lane] = wei - we;
+        }
         if (lane == 7)
         {
             s_base[0] = (wi & 0xFFFFu) ? atomicAdd(&a.counters[0], wi & 0xFFFFu) : 0u;
             s_base[1] = (wi >> 16) ? atomicAdd(&a.counters[4], wi >> 16) : 0u;
+            s_base[2] = wei ? atomicAdd(&a.counters[5], wei) : 0u;
         }
     }
     __syncthreads();
@@ -270,20 +297,28 @@ __global__ void __launch_bounds__(256) k_setup(PassArgs a)
             a.clip_list[q] = gi;
     }
     const uint32_t base = s_base[0] + (excl & 0xFFFFu);
+    const uint32_t slot = s_base[2] + s_went[warp] + eincl - nent;
+    const bool stored = nOut && base < a.rtri_capacity;
     if (gi < a.total_tris)
-        a.tri_first[gi] = (nOut && base < a.rtri_capacity) ? base : kNoTriangle;  // k_clip sets clipped ones
-    if (nOut == 0)
-        return;
-    if (base >= a.rtri_capacity)
+        a.tri_first[gi] = stored ? base : kNoTriangle;  // k_clip sets clipped ones
+    if (nOut && !stored)
     {
         atomicOr(&a.status->overflow, 2u);
-        return;
+        // the reserved entry slots stay in the list, empty
+        for (uint32_t k = 0; k < nent; k++)
+            if (slot + k < a.bin_capacity)
+                a.bin_tmp[slot + k] = make_uint2(kEmptySlot, 0u);
     }
-    t.order = tri << 4;
-    t.meta |= fi << 12;
-    t.poly = kUnclipped;
-    a.rtris[base] = t;
-    bin_count(a, a.frames[fi], base, t);
+    if (stored)
+    {
+        t.order = tri << 4;
+        t.meta |= fi << 12;
+        t.poly = kUnclipped;
+        a.rtris[base] = t;
+    }
+    bin_big_append(a, base, stored && big);
+    if (stored && nent)
+        bin_small(a, a.frames[fi], base, st, slot);
 }
 
 // Clipping of the queued triangles (Clipper.h:107-171): Sutherland-Hodgman,
@@ -357,42 +392,41 @@ __global__ void __launch_bounds__(128) k_clip(PassArgs a)
             tk.meta |= fi << 12;
             tk.poly = (pi << 4) | (uint32_t)k;
             a.rtris[out] = tk;
-            bin_count(a, f, out, tk);
+            const BinGeom g = bin_geom(tk, f);
+            bin_big_append(a, out, !g.small);
+            SmallTiles st;
+            const uint32_t nent = g.small ? small_tiles(f, tk, g, st) : 0u;
+            if (nent)
+                bin_small(a, f, out, st, atomicAdd(&a.counters[5], nent));
             out++;
         }
     }
 }
 
-// Scatter of the decided entries of big triangles into their bins (after
-// the scan).  The list holds one triangle's tiles in a row, all different,
-// so each entry takes its own atomic; empty slots are skipped.
+// Scatter of the unsorted entries into their bins (after the scan); empty
+// slots are skipped.  Lanes with equal tiles share one atomic.
 __global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
 {
     const uint32_t n = *(volatile uint32_t*)&a.counters[5];
     const uint32_t m = (uint32_t)min((uint64_t)n, a.bin_capacity);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (m + stride - 1) / stride;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t r = 0; r < rounds; r++)
     {
-        const uint2 e = a.bin_tmp[i];
+        const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const uint2 e = i < m ? a.bin_tmp[i] : make_uint2(kEmptySlot, 0u);
+        const uint32_t peers = __match_any_sync(0xffffffffu, e.x);
         if (e.x == kEmptySlot)
             continue;
-        const uint64_t pos = (uint64_t)a.tile_offset[e.x] + atomicAdd(&a.tile_cursor[e.x], 1u);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader)
+            base = atomicAdd(&a.tile_cursor[e.x], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+        const uint64_t pos = (uint64_t)a.tile_offset[e.x] + base;
         if (pos < a.bin_capacity)
             a.bins[pos] = e.y;
-    }
-}
-
-// Scatter pass of the small triangles (after the scan).
-__global__ void __launch_bounds__(256) k_bin_scatter(PassArgs a)
-{
-    const uint32_t n = *(volatile uint32_t*)&a.counters[0];
-    const uint32_t nr = min(n, a.rtri_capacity);
-    for (uint32_t ri = blockIdx.x * blockDim.x + threadIdx.x; ri < nr; ri += gridDim.x * blockDim.x)
-    {
-        const RTri t = a.rtris[ri];
-        const FrameDesc& f = a.frames[t.meta >> 12];
-        const BinGeom g = bin_geom(t, f);
-        if (g.small)
-            bin_small<1>(a, f, ri, t, g);
     }
 }
 
@@ -1132,9 +1166,7 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
     k_scan_spine<<<1, 1024, 0, s>>>(block_sums, nscan);
     k_scan_add<<<(a.total_tiles + 255) / 256 + 1, 256, 0, s>>>(a, block_sums, nscan);
     mark(3);
-    const int bin_blocks = sms * (a.tune.bin_blocks_per_sm > 0 ? a.tune.bin_blocks_per_sm : 8);
-    k_bin_scatter<<<bin_blocks, 256, 0, s>>>(a);
-    k_bin_move<<<sms * 4, 256, 0, s>>>(a);
+    k_bin_move<<<sms * (a.tune.bin_blocks_per_sm > 0 ? a.tune.bin_blocks_per_sm : 8), 256, 0, s>>>(a);
     mark(4);
     if (a.tune.raster_variant == 2)
         k_raster<6, false><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
@@ -1148,7 +1180,7 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
 
 int kernels_per_pass(const PassArgs& a)
 {
-    return 8 + (a.total_tris ? 2 : 0);
+    return 7 + (a.total_tris ? 2 : 0);
 }
 
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s)
