@@ -388,7 +388,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     }
     r->rtri_cap = std::min<uint64_t>(r->rtri_cap, 0xFFFFFFF0u);
     const uint64_t rcap = r->rtri_cap, pcap = r->poly_cap;
-    const uint64_t nscan = (tiles + 4095) / 4096;
+    const uint64_t nscan = scan_blocks(tiles);
     EDXR_CUDA(r->frames.ensure(sizeof(FrameDesc) * n));
     EDXR_CUDA(r->tri_first.ensure(4 * std::max<uint64_t>(tt, 1)));
     EDXR_CUDA(r->rtris.ensure(sizeof(RTri) * rcap));
@@ -396,11 +396,11 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     EDXR_CUDA(r->clip_list.ensure(4 * pcap));
     EDXR_CUDA(r->tile_count.ensure(4 * (tiles + 1)));
     EDXR_CUDA(r->tile_offset.ensure(4 * (tiles + 1)));
-    EDXR_CUDA(r->tile_cursor.ensure(4 * (tiles + 1 + nscan + 1)));
+    EDXR_CUDA(r->tile_cursor.ensure(4 * (tiles + 1)));
     EDXR_CUDA(r->bins.ensure(4 * r->bin_capacity));
     EDXR_CUDA(r->bin_tmp.ensure(8 * r->bin_capacity));
     EDXR_CUDA(r->big_list.ensure(4 * r->big_cap));
-    EDXR_CUDA(r->counters.ensure(4 * 8));
+    EDXR_CUDA(r->counters.ensure(4 * kCounters + 8 * std::max<uint64_t>(nscan, 1)));  // + scan status words
     EDXR_CUDA(r->status.ensure(sizeof(DeviceStatus)));
     EDXR_CUDA(r->color.ensure(16 * std::max<uint64_t>(pixels, 1)));
     EDXR_CUDA(r->depth.ensure(4 * std::max<uint64_t>(pixels, 1)));
@@ -433,6 +433,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.big_list = r->big_list.as<uint32_t>();
     a.big_capacity = (uint32_t)r->big_cap;
     a.counters = r->counters.as<uint32_t>();
+    a.scan_status = reinterpret_cast<unsigned long long*>(a.counters + kCounters);
     a.status = r->status.as<DeviceStatus>();
     a.color = r->color.as<float4>();
     a.depth = r->depth.as<float>();

@@ -25,6 +25,15 @@ constexpr uint32_t kNoTriangle = 0xFFFFFFFFu;
 // more entries is split into several items whose winners are merged in a
 // per-pixel key buffer before the last of them shades the tile.
 constexpr uint32_t kItemEntries = 256;
+// Tile-count scan: tiles per block, and blocks (one status word each) of a pass.
+constexpr int kScanItems = 4;
+constexpr int kScanThreads = 1024;
+constexpr int kScanBlock = kScanItems * kScanThreads;
+__host__ __device__ constexpr uint32_t scan_blocks(uint64_t tiles)
+{
+    return (uint32_t)((tiles + kScanBlock - 1) / kScanBlock);
+}
+constexpr int kCounters = 16;  // words of PassArgs::counters
 // Work items of a pass: one per tile plus one per kItemEntries bin entries.
 constexpr uint64_t item_capacity(uint64_t tiles, uint64_t bin_capacity) { return tiles + bin_capacity / kItemEntries + 1; }
 // 3 + one vertex per clip plane is 9 in exact arithmetic; rounding on nearly
@@ -121,14 +130,16 @@ struct PassArgs
     uint32_t* clip_list;     // input triangles (flattened) that straddle a clip plane
     uint32_t* tile_count;    // total_tiles + 1
     uint32_t* tile_offset;   // total_tiles + 1 (exclusive scan of padded counts)
-    uint32_t* tile_cursor;   // total_tiles; the scatter's cursors, then entries of split tiles not yet rastered
+    uint32_t* tile_cursor;   // total_tiles + 1; the scatter's cursors, then entries of split tiles not yet rastered
     uint32_t* bins;
     uint2* bin_tmp;          // decided (tile, entry) pairs before the scatter, bin_capacity of them
     uint64_t bin_capacity;
     uint32_t* big_list;      // raster triangles with many tiles, binned by whole blocks
     uint32_t big_capacity;
     uint32_t* counters;      // [0] raster tris, [1] polys, [2] big tris, [3] raster work queue, [4] clip list,
-                             // [5] decided bin entries, [6] heavy raster work items, [7] light ones
+                             // [5] unsorted bin list slots, [6] heavy raster work items, [7] light ones,
+                             // [8] scan block tickets (kCounters words)
+    unsigned long long* scan_status;  // per scan block (scan_blocks(total_tiles) words)
     uint2* items;            // raster work items (tile, index of its kItemEntries-entry slice): heavy ones
                              // from the front, light ones from the back
     uint64_t item_capacity;

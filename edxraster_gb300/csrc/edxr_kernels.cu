@@ -23,9 +23,6 @@ constexpr int kRasterThreads = 256;    // 8 warps, each on its own work items
 constexpr uint32_t kBigChunk = 128;    // unsorted-list slots a k_bin_big warp reserves at a time
 constexpr uint32_t kEmptySlot = 0xFFFFFFFFu;
 constexpr uint32_t kHeavyItem = 64;    // raster items with this many entries are handed out first
-constexpr int kScanItems = 4;
-constexpr int kScanThreads = 1024;
-constexpr int kScanBlock = kScanItems * kScanThreads;
 
 // -------------------------------------------------------------------------
 __global__ void k_clear(PassArgs a)
@@ -36,8 +33,10 @@ __global__ void k_clear(PassArgs a)
         a.tile_count[i] = 0;
         a.tile_cursor[i] = 0;
     }
-    if (blockIdx.x == 0 && threadIdx.x < 8)
+    if (blockIdx.x == 0 && threadIdx.x < kCounters)
         a.counters[threadIdx.x] = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < scan_blocks(a.total_tiles); i += stride)
+        a.scan_status[i] = 0ull;
     if (blockIdx.x == 0 && threadIdx.x == 0)
     {
         a.status->overflow = 0;
@@ -510,156 +509,185 @@ __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
 
 // -------------------------------------------------------------------------
 // Exclusive scan of the per-tile counts, each rounded up to a multiple of 4
-// entries so every bin starts on a 16-byte boundary.
+// entries so every bin starts on a 16-byte boundary, in one pass: blocks
+// take consecutive ranges of kScanBlock tiles in the order they start (a
+// ticket, so every range a block waits for belongs to a block already
+// running) and find their offset by looking back over the published sums of
+// the ranges before them (scan_status: 0 not yet, kScanAggregate | sum of
+// the range, kScanPrefix | sum of everything up to the range's end).
+//
+// The same pass lists the raster work items: one per tile (an empty tile's
+// item writes its background) plus one per further kItemEntries entries.
+// Items of at least kHeavyItem entries are listed from the front of the
+// item array, the lighter ones from its back, and the queue hands out the
+// front list first: the heavy work starts early instead of forming the tail.
 __device__ __forceinline__ uint32_t padded(uint32_t c) { return (c + 3u) & ~3u; }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_blocks(PassArgs a, uint32_t* block_sums)
-{
-    __shared__ uint32_t warp_sums[kScanThreads / 32];
-    const uint32_t base = blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
-    uint32_t v[kScanItems], s = 0;
-#pragma unroll
-    for (int k = 0; k < kScanItems; k++)
-    {
-        const uint32_t i = base + k;
-        v[k] = (i < a.total_tiles) ? padded(a.tile_count[i]) : 0u;
-        s += v[k];
-    }
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t incl = s;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= (uint32_t)o) incl += t;
-    }
-    if (lane == 31) warp_sums[warp] = incl;
-    __syncthreads();
-    if (warp == 0)
-    {
-        uint32_t w = warp_sums[lane];
-        uint32_t wi = w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= (uint32_t)o) wi += t;
-        }
-        warp_sums[lane] = wi - w;
-        if (lane == 31) block_sums[blockIdx.x] = wi;
-    }
-    __syncthreads();
-    uint32_t run = warp_sums[warp] + incl - s;
-#pragma unroll
-    for (int k = 0; k < kScanItems; k++)
-    {
-        const uint32_t i = base + k;
-        if (i < a.total_tiles) a.tile_offset[i] = run;
-        run += v[k];
-    }
-}
+constexpr unsigned long long kScanAggregate = 1ull << 32;
+constexpr unsigned long long kScanPrefix = 2ull << 32;
+constexpr int kScanSpinLimit = 1 << 22;
 
-__global__ void __launch_bounds__(1024) k_scan_spine(uint32_t* block_sums, uint32_t nblocks)
+// Block-wide inclusive scan of one value per thread; returns the inclusive
+// value and sets `total` (all threads).
+__device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* warp_sums, uint32_t& total)
 {
-    // single block; nblocks <= 1024 * 4
-    __shared__ uint32_t warp_sums[32];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t v[4], s = 0;
-    for (int k = 0; k < 4; k++)
-    {
-        const uint32_t i = threadIdx.x * 4 + k;
-        v[k] = i < nblocks ? block_sums[i] : 0u;
-        s += v[k];
-    }
-    uint32_t incl = s;
+    uint32_t incl = v;
+#pragma unroll
     for (int o = 1; o < 32; o <<= 1)
     {
         const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= (uint32_t)o) incl += t;
     }
-    if (lane == 31) warp_sums[warp] = incl;
+    if (lane == 31)
+        warp_sums[warp] = incl;
     __syncthreads();
     if (warp == 0)
     {
         const uint32_t w = warp_sums[lane];
         uint32_t wi = w;
+#pragma unroll
         for (int o = 1; o < 32; o <<= 1)
         {
             const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
             if (lane >= (uint32_t)o) wi += t;
         }
         warp_sums[lane] = wi - w;
+        if (lane == 31)
+            warp_sums[32] = wi;
     }
     __syncthreads();
-    uint32_t run = warp_sums[warp] + incl - s;
-    for (int k = 0; k < 4; k++)
-    {
-        const uint32_t i = threadIdx.x * 4 + k;
-        if (i < nblocks) block_sums[i] = run;  // exclusive
-        run += v[k];
-    }
-    if (threadIdx.x == blockDim.x - 1)
-        block_sums[nblocks] = run;  // grand total
+    total = warp_sums[32];
+    return warp_sums[warp] + incl;
 }
 
-// Final offsets, and the raster work items: one per tile (an empty tile's
-// item writes its background) plus one per further kItemEntries entries.
-// Items of at least kHeavyItem entries are listed from the front of the
-// item array, the lighter ones from its back, and the queue hands out the
-// front list first: the heavy work starts early instead of forming the tail.
-__global__ void k_scan_add(PassArgs a, const uint32_t* block_sums, uint32_t nblocks)
+__global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t count = 0, n = 0;
-    if (i < a.total_tiles)
+    __shared__ uint32_t warp_sums[33];
+    __shared__ uint32_t s_block, s_prefix;
+    if (threadIdx.x == 0)
+        s_block = atomicAdd(&a.counters[8], 1u);
+    __syncthreads();
+    const uint32_t b = s_block;
+    const uint32_t base = b * kScanBlock + threadIdx.x * kScanItems;
+    uint32_t cnt[kScanItems], sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++)
     {
-        const uint32_t start = a.tile_offset[i] + block_sums[i / kScanBlock];
-        a.tile_offset[i] = start;
-        count = a.tile_count[i];
-        if ((uint64_t)start + count > a.bin_capacity)
-            count = 0;  // overflowed frame: k_raster skips the tile's entries too
-        n = max(1u, (count + kItemEntries - 1) / kItemEntries);
+        const uint32_t i = base + k;
+        cnt[k] = (i < a.total_tiles) ? a.tile_count[i] : 0u;
+        sum += padded(cnt[k]);
     }
-    // only the last item of a tile can be light
-    const uint32_t last = count - (n - 1) * kItemEntries;
-    const uint32_t nlight = (i < a.total_tiles && last < kHeavyItem) ? 1u : 0u;
-    const uint32_t nheavy = n - nlight;
-    // one atomic per warp and list for the items of its 32 tiles (heavy
-    // count in the low half, light count in the high half)
+    uint32_t total;
+    const uint32_t incl = block_scan(sum, warp_sums, total);
+    if (threadIdx.x == 0)
+    {
+        uint32_t prefix = 0;
+        if (b == 0)
+            atomicExch(&a.scan_status[0], kScanPrefix | total);
+        else
+        {
+            atomicExch(&a.scan_status[b], kScanAggregate | total);
+            for (int j = (int)b - 1; j >= 0;)
+            {
+                unsigned long long st = 0;
+                int spins = 0;
+                do
+                    st = *(volatile unsigned long long*)&a.scan_status[j];
+                while (st == 0 && ++spins < kScanSpinLimit);
+                if (st == 0)
+                {
+                    // a range never published: report it, never hang
+                    atomicOr(&a.status->error, 3u);  // EDXR_ERR_TIMEOUT
+                    break;
+                }
+                prefix += (uint32_t)st;
+                if (st & kScanPrefix)
+                    break;
+                j--;
+            }
+            atomicExch(&a.scan_status[b], kScanPrefix | (prefix + total));
+        }
+        s_prefix = prefix;
+    }
+    __syncthreads();
+    const uint32_t prefix = s_prefix;
+
+    // offsets, and the items of this thread's tiles
+    uint32_t run = prefix + incl - sum;
+    uint32_t nheavy = 0, nlight = 0;
+    uint32_t start[kScanItems], n[kScanItems];
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++)
+    {
+        const uint32_t i = base + k;
+        start[k] = run;
+        n[k] = 0;
+        if (i < a.total_tiles)
+        {
+            a.tile_offset[i] = run;
+            uint32_t c = cnt[k];
+            if ((uint64_t)run + c > a.bin_capacity)
+                c = 0;  // overflowed frame: k_raster skips the tile's entries too
+            n[k] = max(1u, (c + kItemEntries - 1) / kItemEntries);
+            // only the last item of a tile can be light
+            const uint32_t light = (c - (n[k] - 1) * kItemEntries) < kHeavyItem ? 1u : 0u;
+            nlight += light;
+            nheavy += n[k] - light;
+            cnt[k] = c;
+        }
+        run += padded(cnt[k]);
+    }
+    // one atomic per warp and list (heavy count in the low half, light
+    // count in the high half of one word: at most 32 * 4 * 2^8 and 128)
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t packed = nheavy | (nlight << 16);
-    uint32_t incl = packed;
+    const uint32_t packed = nheavy | (nlight << 24);
+    uint32_t pincl = packed;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1)
     {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= (uint32_t)o) incl += t;
+        const uint32_t t = __shfl_up_sync(0xffffffffu, pincl, o);
+        if (lane >= (uint32_t)o) pincl += t;
     }
     uint32_t hbase = 0, lbase = 0;
     if (lane == 31)
     {
-        if (incl & 0xFFFFu)
-            hbase = atomicAdd(&a.counters[6], incl & 0xFFFFu);
-        if (incl >> 16)
-            lbase = atomicAdd(&a.counters[7], incl >> 16);
+        if (pincl & 0xFFFFFFu)
+            hbase = atomicAdd(&a.counters[6], pincl & 0xFFFFFFu);
+        if (pincl >> 24)
+            lbase = atomicAdd(&a.counters[7], pincl >> 24);
     }
-    const uint32_t excl = incl - packed;
-    hbase = __shfl_sync(0xffffffffu, hbase, 31) + (excl & 0xFFFFu);
-    lbase = __shfl_sync(0xffffffffu, lbase, 31) + (excl >> 16);
-    for (uint32_t j = 0; j < nheavy; j++)
-        if (hbase + j < a.item_capacity)
-            a.items[hbase + j] = make_uint2(i, j);
-    if (nlight && lbase < a.item_capacity)
-        a.items[a.item_capacity - 1 - lbase] = make_uint2(i, n - 1);
-    if (i == 0)
+    const uint32_t pexcl = pincl - packed;
+    hbase = __shfl_sync(0xffffffffu, hbase, 31) + (pexcl & 0xFFFFFFu);
+    lbase = __shfl_sync(0xffffffffu, lbase, 31) + (pexcl >> 24);
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++)
     {
-        const uint64_t total = block_sums[nblocks];
-        a.tile_offset[a.total_tiles] = (uint32_t)total;
-        // the unsorted list of big-triangle entries shares the capacity
-        const uint64_t needed = max(total, (uint64_t)a.counters[5]);
+        const uint32_t i = base + k;
+        if (i >= a.total_tiles)
+            continue;
+        const bool light = (cnt[k] - (n[k] - 1) * kItemEntries) < kHeavyItem;
+        const uint32_t heavy = n[k] - (light ? 1u : 0u);
+        for (uint32_t j = 0; j < heavy; j++, hbase++)
+            if (hbase < a.item_capacity)
+                a.items[hbase] = make_uint2(i, j);
+        if (light)
+        {
+            if (lbase < a.item_capacity)
+                a.items[a.item_capacity - 1 - lbase] = make_uint2(i, n[k] - 1);
+            lbase++;
+        }
+    }
+
+    // the range holding the last tile has the grand total
+    if (a.total_tiles > 0 && b == (a.total_tiles - 1) / kScanBlock && threadIdx.x == kScanThreads - 1)
+    {
+        const uint64_t grand = prefix + total;
+        a.tile_offset[a.total_tiles] = (uint32_t)grand;
+        // the unsorted list shares the capacity
+        const uint64_t needed = max(grand, (uint64_t)a.counters[5]);
         a.status->bins_needed = needed;
         a.status->raster_tris = a.counters[0];
-        a.status->clipped_polys = a.counters[1];
         a.status->big_tris = a.counters[2];
         if (a.counters[0] > a.rtri_capacity)
             atomicOr(&a.status->overflow, 2u);
@@ -682,9 +710,9 @@ __global__ void k_scan_add(PassArgs a, const uint32_t* block_sums, uint32_t nblo
 // fragment with the smallest depth wins, for LESS the first.  Keys can be
 // combined in any order, so the bin needs no ordering and two paths share
 // the work of each group of 32 entries (one staged per lane):
-//  * small entries (quad-aligned region of at most tune.small_region pixels)
-//    are rasterized triangle-parallel by the lane that staged them, merging
-//    into the key array with a shared 64-bit atomicMin;
+//  * small entries (region of at most tune.small_region pixels): their
+//    (entry, pixel) pairs are spread over the lanes, merging into the key
+//    array with a shared 64-bit atomicMin;
 //  * the other entries are staged as tile-relative edge equations and
 //    rasterized pixel-parallel by the whole warp over their region.
 // Entries whose depth lower bound is behind every pixel of the tile so far
@@ -1147,8 +1175,7 @@ Tuning default_tuning()
 cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
 {
     const int sms = a.num_sms > 0 ? a.num_sms : 148;
-    const uint32_t nscan = (a.total_tiles + kScanBlock - 1) / kScanBlock;
-    uint32_t* block_sums = a.tile_cursor + a.total_tiles + 1;  // scratch after the cursors
+    const uint32_t nscan = scan_blocks(a.total_tiles);
     auto mark = [&](int i) {
         if (ev) cudaEventRecord(ev[i], s);
     };
@@ -1162,9 +1189,7 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
     }
     k_bin_big<<<sms * 4, 256, 0, s>>>(a);
     mark(2);
-    k_scan_blocks<<<nscan, kScanThreads, 0, s>>>(a, block_sums);
-    k_scan_spine<<<1, 1024, 0, s>>>(block_sums, nscan);
-    k_scan_add<<<(a.total_tiles + 255) / 256 + 1, 256, 0, s>>>(a, block_sums, nscan);
+    k_scan<<<nscan, kScanThreads, 0, s>>>(a);
     mark(3);
     k_bin_move<<<sms * (a.tune.bin_blocks_per_sm > 0 ? a.tune.bin_blocks_per_sm : 8), 256, 0, s>>>(a);
     mark(4);
@@ -1180,7 +1205,7 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
 
 int kernels_per_pass(const PassArgs& a)
 {
-    return 7 + (a.total_tris ? 2 : 0);
+    return 5 + (a.total_tris ? 2 : 0);
 }
 
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s)

@@ -58,11 +58,11 @@ constexpr size_t kOffClipList = align256(kOffPoly + sizeof(ClipPoly) * (size_t)k
 constexpr size_t kOffCount = align256(kOffClipList + 4 * (size_t)kPolyCap);
 constexpr size_t kOffOffset = align256(kOffCount + 4 * (size_t)(kMaxTiles + 1));
 constexpr size_t kOffCursor = align256(kOffOffset + 4 * (size_t)(kMaxTiles + 1));
-constexpr size_t kOffBins = align256(kOffCursor + 4 * (size_t)(kMaxTiles + 1 + 8));
+constexpr size_t kOffBins = align256(kOffCursor + 4 * (size_t)(kMaxTiles + 1));
 constexpr size_t kOffBinTmp = align256(kOffBins + 4 * (size_t)kBinCap);
 constexpr size_t kOffBig = align256(kOffBinTmp + 8 * (size_t)kBinCap);
 constexpr size_t kOffCounters = align256(kOffBig + 4 * (size_t)kBigCap);
-constexpr size_t kOffStatus = align256(kOffCounters + 4 * 8);
+constexpr size_t kOffStatus = align256(kOffCounters + 4 * kCounters + 8 * (size_t)scan_blocks(kMaxTiles));
 constexpr size_t kOffTriFirst = align256(kOffStatus + sizeof(DeviceStatus));
 constexpr size_t kItemCap = item_capacity(kMaxTiles, kBinCap);
 constexpr size_t kOffItems = align256(kOffTriFirst + 4 * (size_t)kMaxTriangles);
@@ -260,6 +260,7 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
     a.big_list = reinterpret_cast<uint32_t*>(base + kOffBig);
     a.big_capacity = kBigCap;
     a.counters = reinterpret_cast<uint32_t*>(base + kOffCounters);
+    a.scan_status = reinterpret_cast<unsigned long long*>(a.counters + kCounters);
     a.status = reinterpret_cast<DeviceStatus*>(base + kOffStatus);
     a.color = reinterpret_cast<float4*>(color);
     a.depth = depth;
