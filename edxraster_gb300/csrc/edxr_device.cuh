@@ -287,18 +287,16 @@ __device__ __forceinline__ int edge_scalar(const Edges& e, int k, int px, int py
                 tl_scalar(e.vx[k], e.vy[k], e.vx[n], e.vy[n]));
 }
 
-// Lane q of GenStepVectors (RasterTriangle.h:192-255) for one edge.
+// Lane q of GenStepVectors (RasterTriangle.h:192-255) for one edge: from
+// the tested corner (cx, cy) = (corner & 1, corner >> 1) to the same corner
+// of quadrant (qx, qy) = (q & 1, q >> 1), (qx - cx) * B + (qy - cy) * C, in
+// steps of stepSize = blockSize << 3 = 256 (blockSize = 32).  The table of
+// the reference lists exactly these sums; int32 arithmetic wraps the same
+// way in either order.
 __device__ __forceinline__ int step_lane(uint32_t corner, int B, int C, int q)
 {
-    int v;
-    switch (corner)
-    {
-    case 0: v = (q == 0) ? 0 : (q == 1) ? B : (q == 2) ? C : wadd(B, C); break;
-    case 1: v = (q == 0) ? wsub(0, B) : (q == 1) ? 0 : (q == 2) ? wsub(C, B) : C; break;
-    case 2: v = (q == 0) ? wsub(0, C) : (q == 1) ? wsub(B, C) : (q == 2) ? 0 : B; break;
-    default: v = (q == 0) ? wsub(wsub(0, B), C) : (q == 1) ? wsub(0, C) : (q == 2) ? wsub(0, B) : 0; break;
-    }
-    return wmul(256, v);  // stepSize = blockSize << 3 with blockSize = 32
+    const int dx = (q & 1) - (int)(corner & 1), dy = (q >> 1) - (int)(corner >> 1);
+    return wmul(256, wadd(wmul(dx, B), wmul(dy, C)));
 }
 
 // Per-triangle binning geometry.

@@ -429,11 +429,13 @@ __global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
     }
 }
 
-// One warp per triangle of the big list; lanes take 32x32 tiles.  Each
-// entry is counted in its tile and kept in the unsorted list, which the
-// warp fills from slots it reserves kBigChunk at a time (one atomic on the
-// shared counter per chunk instead of one per group of 32 candidates);
-// slots it leaves unused are marked empty.
+// Big triangles, up to 32 at a time per warp: their (triangle, 32x32 reference
+// tile) pairs are numbered across the warp and taken 32 at a time, each lane
+// deciding the four quadrants of its pair's tile, so a triangle with few
+// tiles does not leave lanes idle.  Each entry is counted in its tile and
+// kept in the unsorted list, which the warp fills from slots it reserves
+// kBigChunk at a time (one atomic on the shared counter per chunk); slots
+// it leaves unused are marked empty.
 __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
 {
     const uint32_t nb = min(*(volatile uint32_t*)&a.counters[2], a.big_capacity);
@@ -445,36 +447,65 @@ __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
             if (cbase + k < a.bin_capacity)
                 a.bin_tmp[cbase + k] = make_uint2(kEmptySlot, 0u);
     };
-    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nb; b += nw)
+    // batches of up to 32 triangles, small enough that every warp gets one
+    const uint32_t batch = min(32u, max(1u, (nb + nw - 1) / nw));
+    for (uint32_t b0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * batch; b0 < nb; b0 += nw * batch)
     {
-        const uint32_t ri = a.big_list[b];
-        const RTri t = a.rtris[ri];
-        const FrameDesc& f = a.frames[t.meta >> 12];
-        const BinGeom g = bin_geom(t, f);
-        const Edges e = tri_edges(t);
-        // lanes take 32x32 reference tiles and decide their four quadrants
-        const int nx = g.t32x1 - g.t32x0 + 1, ny = g.t32y1 - g.t32y0 + 1;
-        for (int j0 = 0; j0 < nx * ny; j0 += 32)
+        // this lane's triangle of the batch and its number of 32x32 tiles
+        uint32_t mine = kNoTriangle;
+        int n = 0;
+        if (lane < batch && b0 + lane < nb)
         {
-            const int j = j0 + (int)lane;
-            uint32_t dq = 0;
-            int T32x = 0, T32y = 0;
-            if (j < nx * ny)
+            mine = a.big_list[b0 + lane];
+            const RTri t = a.rtris[mine];
+            const BinGeom g = bin_geom(t, a.frames[t.meta >> 12]);
+            n = (g.t32x1 - g.t32x0 + 1) * (g.t32y1 - g.t32y0 + 1);
+        }
+        int incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += v;
+        }
+        const int pairs = __shfl_sync(0xffffffffu, incl, 31);
+        for (int base = 0; base < pairs; base += 32)
+        {
+            const int p = base + (int)lane;
+            // owner: the first lane whose inclusive count exceeds p
+            int j = 0;
+#pragma unroll
+            for (int st = 16; st >= 1; st >>= 1)
             {
-                T32x = g.t32x0 + j % nx;
-                T32y = g.t32y0 + j / nx;
+                const int v = __shfl_sync(0xffffffffu, incl, j + st - 1);
+                if (v <= p) j += st;
+            }
+            const int first = __shfl_sync(0xffffffffu, incl - n, j);
+            const uint32_t ri = __shfl_sync(0xffffffffu, mine, j);
+            uint32_t dq = 0, tile00 = 0;
+            int tdx = 0;
+            if (p < pairs)
+            {
+                const RTri t = a.rtris[ri];
+                const FrameDesc& f = a.frames[t.meta >> 12];
+                const BinGeom g = bin_geom(t, f);
+                const Edges e = tri_edges(t);
+                const int nx = g.t32x1 - g.t32x0 + 1, local = p - first;
+                const int T32y = g.t32y0 + local / nx, T32x = g.t32x0 + local - (local / nx) * nx;
                 dq = quad_decisions(t, e, g, f, T32x, T32y);
+                tdx = f.tdx;
+                tile00 = f.tile_base + (uint32_t)(2 * T32y * f.tdx + 2 * T32x);
             }
             const uint32_t nz = (dq | (dq >> 1)) & 0x55u;
             const int cnt = __popc(nz);
-            int incl = cnt;
+            int cincl = cnt;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1)
             {
-                const int v = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= (uint32_t)o) incl += v;
+                const int v = __shfl_up_sync(0xffffffffu, cincl, o);
+                if (lane >= (uint32_t)o) cincl += v;
             }
-            const uint32_t h = (uint32_t)__shfl_sync(0xffffffffu, incl, 31);
+            const uint32_t h = (uint32_t)__shfl_sync(0xffffffffu, cincl, 31);
             if (h == 0)
                 continue;
             if (h > cleft)
@@ -486,15 +517,14 @@ __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
                 cbase = __shfl_sync(0xffffffffu, nbase, 0);
                 cleft = kBigChunk;
             }
-            uint32_t pos = cbase + (uint32_t)(incl - cnt);
+            uint32_t pos = cbase + (uint32_t)(cincl - cnt);
 #pragma unroll
             for (int q = 0; q < 4; q++)
             {
                 const uint32_t d = (dq >> (2 * q)) & 3u;
                 if (!d)
                     continue;
-                const int tx = 2 * T32x + (q & 1), ty = 2 * T32y + (q >> 1);
-                const uint32_t tile = f.tile_base + (uint32_t)(ty * f.tdx + tx);
+                const uint32_t tile = tile00 + (uint32_t)((q >> 1) * tdx + (q & 1));
                 atomicAdd(&a.tile_count[tile], 1u);
                 if (pos < a.bin_capacity)
                     a.bin_tmp[pos] = make_uint2(tile, (ri << 2) | d);
