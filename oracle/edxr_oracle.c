@@ -266,8 +266,10 @@ typedef struct
     int tdx, tdy;      /* 32x32 tile grid */
     long long* refStart; /* per tile */
     triref* refs;
-    /* padded per-pixel state, (tdx*32) x (tdy*32) */
+    /* padded per-pixel state, (tdx*32) x (tdy*32), one plane per sample */
     int pw, ph;
+    int S;             /* samples per pixel */
+    size_t npad;       /* pixels of one plane */
     float* depth;
     int* win;          /* raster triangle index or -1 */
     float* l0; float* l1;
@@ -598,6 +600,111 @@ static void quad_fragment(frame* f, const rtri* t, int ti, int x, int y, const i
         f->tileFrags[(y >> TILE_LOG2) * f->tdx + (x >> TILE_LOG2)]++;
 }
 
+/* FrameBuffer::MultiSampleOffsets (FrameBuffer.cpp:107-191): the table of
+ * 1/16-pixel sample offsets, per sample-count log2, as the reference lists
+ * it.  The rasterizer reads sample s as `const Vector2i& sampleOffset =
+ * MultiSampleOffsets[level][2 * s]` (Rasterizer.h:247, 382): an int bound to
+ * a Vector2i reference goes through Vector2i's scalar constructor, so the
+ * sample sits at (t[2s], t[2s]) from the pixel centre.  sample_offset() is
+ * that value. */
+static const int kSampleOffsets[6][64] = {
+    { 0, 0 },
+    { 4, 4, -4, -4 },
+    { -2, -6, 6, -2, -6, 2, 2, 6 },
+    { 1, -3, -1, 3, 5, 1, -3, -5, -5, 5, -7, -1, 3, 7, 7, -7 },
+    { 1, 1, -1, -3, -3, 2, 4, -1, -5, -2, 2, 5, 5, 3, 3, -5,
+      -2, 6, 0, -7, -4, -6, -6, 4, -8, 0, 7, -4, 6, 7, -7, -8 },
+    { 1, 1, -1, -3, -3, 2, 4, -1, -5, -2, 2, 5, 5, 3, 3, -5,
+      -2, 6, 0, -7, -4, -6, -6, 4, -8, 0, 7, -4, 6, 7, -7, -8,
+      1, 3, -3, -3, -3, 0, 6, -2, -7, -1, 3, 4, 7, 3, 3, -6,
+      -2, 7, 0, -4, -2, -5, -7, 6, -8, 3, 4, -1, 2, 7, 4, -8 }
+};
+
+static inline int sample_offset(int level, int s) { return kSampleOffsets[level][2 * s]; }
+
+/* Depth test of one sample at 1/16-pixel position (sx, sy) (ZTestQuad with a
+ * sample id, FrameBuffer.cpp:54-68; the depth from the sample's barycentrics,
+ * RasterTriangle.h:324-337).  Returns whether the sample passed. */
+static int sample_test(frame* f, const rtri* t, int ti, int px, int py, int s, int sx, int sy)
+{
+    const rvert* v0 = &f->rv[t->vid[0]];
+    const rvert* v1 = &f->rv[t->vid[1]];
+    const rvert* v2 = &f->rv[t->vid[2]];
+    const int e1 = wadd(wmul(t->B1, wsub(sx, t->v2x)), wmul(t->C1, wsub(sy, t->v2y)));
+    const int e2 = wadd(wmul(t->B2, wsub(sx, t->v2x)), wmul(t->C2, wsub(sy, t->v2y)));
+    const float l0 = (float)e1 * t->invDet;
+    const float l1 = (float)e2 * t->invDet;
+    const float l2 = (1.0f - l0) - l1;
+    const float d = (l0 * v0->clip.z + l1 * v1->clip.z) + l2 * v2->clip.z;
+    const size_t p = (size_t)s * f->npad + (size_t)py * f->pw + px;
+    const float cur = f->depth[p];
+    const int pass = (f->P->depth_func == EDXR_ORACLE_DEPTH_LESS) ? (d < cur) : (d <= cur);
+    if (pass)
+    {
+        f->depth[p] = d;
+        f->win[p] = ti;
+    }
+    return pass;
+}
+
+/* Rasterizer::FineRasterize_MultiSample, Rasterizer.h:202-300: per sample the
+ * biased pixel-centre edge values plus the sample offset, then the sample's
+ * depth test. */
+static void fine_raster_ms(frame* f, const rtri* t, int ti, int minX, int minY, int maxX, int maxY)
+{
+    static const int offx[4] = { 8, 24, 8, 24 }, offy[4] = { 8, 8, 24, 24 };
+    const int level = f->P->msaa_log2;
+    const int b0 = tl_sse(t->v0x, t->v0y, t->v1x, t->v1y);
+    const int b1 = tl_sse(t->v1x, t->v1y, t->v2x, t->v2y);
+    const int b2 = tl_sse(t->v2x, t->v2y, t->v0x, t->v0y);
+    for (int y = minY; y <= maxY; y += 2)
+        for (int x = minX; x <= maxX; x += 2)
+        {
+            int any = 0;
+            for (int lane = 0; lane < 4; lane++)
+            {
+                const int cx = (x << 4) + offx[lane], cy = (y << 4) + offy[lane];
+                const int e0 = wadd(wadd(wmul(t->B0, wsub(cx, t->v0x)), wmul(t->C0, wsub(cy, t->v0y))), b0);
+                const int e1 = wadd(wadd(wmul(t->B1, wsub(cx, t->v1x)), wmul(t->C1, wsub(cy, t->v1y))), b1);
+                const int e2 = wadd(wadd(wmul(t->B2, wsub(cx, t->v2x)), wmul(t->C2, wsub(cy, t->v2y))), b2);
+                for (int s = 0; s < f->S; s++)
+                {
+                    const int ox = sample_offset(level, s), oy = ox;
+                    const int s0 = wadd(wadd(e0, wmul(ox, t->B0)), wmul(oy, t->C0));
+                    const int s1 = wadd(wadd(e1, wmul(ox, t->B1)), wmul(oy, t->C1));
+                    const int s2 = wadd(wadd(e2, wmul(ox, t->B2)), wmul(oy, t->C2));
+                    if ((s0 | s1 | s2) >= 0)
+                        any |= sample_test(f, t, ti, x + (lane & 1), y + (lane >> 1), s, cx + ox, cy + oy);
+                }
+            }
+            if (any)
+                f->tileFrags[(y >> TILE_LOG2) * f->tdx + (x >> TILE_LOG2)]++;
+        }
+}
+
+/* Rasterizer::TrivialAcceptTriangle_MultiSample, Rasterizer.h:355-415. */
+static void trivial_accept_ms(frame* f, const rtri* t, int ti, int minX, int minY, int maxX, int maxY)
+{
+    static const int offx[4] = { 8, 24, 8, 24 }, offy[4] = { 8, 8, 24, 24 };
+    const int level = f->P->msaa_log2;
+    for (int y = minY; y <= maxY; y += 2)
+        for (int x = minX; x <= maxX; x += 2)
+        {
+            int any = 0;
+            for (int lane = 0; lane < 4; lane++)
+            {
+                const int cx = (x << 4) + offx[lane], cy = (y << 4) + offy[lane];
+                for (int s = 0; s < f->S; s++)
+                {
+                    const int o = sample_offset(level, s);
+                    any |= sample_test(f, t, ti, x + (lane & 1), y + (lane >> 1), s, cx + o, cy + o);
+                }
+            }
+            if (any)
+                f->tileFrags[(y >> TILE_LOG2) * f->tdx + (x >> TILE_LOG2)]++;
+        }
+}
+
 /* Rasterizer::FineRasterize_SingleSample, Rasterizer.h:126-200. */
 static void fine_raster(frame* f, const rtri* t, int ti, int bminx, int bminy, int bmaxx, int bmaxy)
 {
@@ -609,6 +716,11 @@ static void fine_raster(frame* f, const rtri* t, int ti, int bminx, int bminy, i
     minY -= minY % 2;
     if (maxX < minX || maxY < minY)
         return;
+    if (f->S > 1)
+    {
+        fine_raster_ms(f, t, ti, minX, minY, maxX, maxY);
+        return;
+    }
     static const int offx[4] = { 8, 24, 8, 24 }, offy[4] = { 8, 8, 24, 24 };
     const int b0 = tl_sse(t->v0x, t->v0y, t->v1x, t->v1y);
     const int b1 = tl_sse(t->v1x, t->v1y, t->v2x, t->v2y);
@@ -639,6 +751,11 @@ static void trivial_accept(frame* f, const rtri* t, int ti, int bminx, int bminy
     int minX = bminx, maxX = bmaxx - 1, minY = bminy, maxY = bmaxy - 1;
     minX -= minX % 2;
     minY -= minY % 2;
+    if (f->S > 1)
+    {
+        trivial_accept_ms(f, t, ti, minX, minY, maxX, maxY);
+        return;
+    }
     static const int all[4] = { 1, 1, 1, 1 };
     for (int y = minY; y <= maxY; y += 2)
         for (int x = minX; x <= maxX; x += 2)
@@ -858,9 +975,60 @@ typedef struct
     edxr_oracle_out* out;
 } job;
 
+/* Color4b::FromFloats / Color4b(Color) of the shim: clamp, scale by 255,
+ * round half up, all in float. */
+static unsigned char to_byte(float v)
+{
+    v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+    return (unsigned char)(v * 255.0f + 0.5f);
+}
+
+/* One pixel with S > 1 samples: every sample's winner is shaded at the pixel
+ * centre (the fragment's barycentrics, Rasterizer.h:279-281), stored as 8-bit
+ * colour (Renderer.cpp:295-299, 305-350; a sample no fragment reached keeps
+ * the clear value 0), and FrameBuffer::Resolve (FrameBuffer.cpp:70-87)
+ * averages the samples in float. */
+static void shade_pixel_ms(frame* f, edxr_oracle_out* out, int x, int y)
+{
+    const int W = f->P->width, H = f->P->height;
+    const size_t po = (size_t)y * W + x;
+    float acc[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+    for (int s = 0; s < f->S; s++)
+    {
+        const size_t pp = (size_t)s * f->npad + (size_t)y * f->pw + x;
+        const size_t so = (size_t)s * W * H + po;
+        const int ti = f->win[pp];
+        if (out->id) out->id[so] = ti < 0 ? 0xFFFFFFFFu : f->rt[ti].texId;
+        if (out->depth) out->depth[so] = f->depth[pp];
+        if (ti < 0 || !out->color)
+            continue;
+        const rtri* t = &f->rt[ti];
+        const int cx = (x << 4) + 8, cy = (y << 4) + 8;
+        const int e1 = wadd(wmul(t->B1, wsub(cx, t->v2x)), wmul(t->C1, wsub(cy, t->v2y)));
+        const int e2 = wadd(wmul(t->B2, wsub(cx, t->v2x)), wmul(t->C2, wsub(cy, t->v2y)));
+        double rgb[3];
+        shade_pixel(f, ti, (float)e1 * t->invDet, (float)e2 * t->invDet, rgb);
+        for (int q = 0; q < 3; q++)
+            acc[q] += (float)to_byte((float)rgb[q]) / 255.0f;
+        acc[3] += 255.0f / 255.0f;
+    }
+    if (out->color)
+    {
+        const float inv = 1.0f / (float)f->S;
+        for (int q = 0; q < 4; q++)
+            out->color[4 * po + q] = (double)(acc[q] * inv);
+    }
+}
+
 static void shade_row(frame* f, edxr_oracle_out* out, int y)
 {
     const int W = f->P->width;
+    if (f->S > 1)
+    {
+        for (int x = 0; x < W; x++)
+            shade_pixel_ms(f, out, x, y);
+        return;
+    }
     for (int x = 0; x < W; x++)
     {
         const size_t pp = (size_t)y * f->pw + x;
@@ -915,7 +1083,8 @@ static void run_parallel(frame* f, edxr_oracle_out* out, int kind, long long n, 
 
 int edxr_oracle_render(const edxr_oracle_params* P, const edxr_oracle_mesh* M, edxr_oracle_out* out)
 {
-    if (!P || !M || !out || P->width <= 0 || P->height <= 0 || M->nv < 0 || M->nt < 0)
+    if (!P || !M || !out || P->width <= 0 || P->height <= 0 || M->nv < 0 || M->nt < 0 ||
+        P->msaa_log2 < 0 || P->msaa_log2 > 5)
         return -1;
     if (M->nt > 0 && (!M->indices || !M->positions))
         return -1;
@@ -951,18 +1120,21 @@ int edxr_oracle_render(const edxr_oracle_params* P, const edxr_oracle_mesh* M, e
 
     f.pw = f.tdx * TILE_SIZE;
     f.ph = f.tdy * TILE_SIZE;
+    f.S = 1 << P->msaa_log2;
     const size_t npad = (size_t)f.pw * f.ph;
-    f.depth = (float*)malloc(npad * sizeof(float));
-    f.win = (int*)malloc(npad * sizeof(int));
+    f.npad = npad;
+    f.depth = (float*)malloc(npad * f.S * sizeof(float));
+    f.win = (int*)malloc(npad * f.S * sizeof(int));
     f.l0 = (float*)malloc(npad * sizeof(float));
     f.l1 = (float*)malloc(npad * sizeof(float));
     if (!f.depth || !f.win || !f.l0 || !f.l1) goto done;
-    for (size_t i = 0; i < npad; i++)
+    for (size_t i = 0; i < npad * f.S; i++)
     {
         f.depth[i] = 1.0f; /* FrameBuffer::Clear, FrameBuffer.cpp:97-103 */
         f.win[i] = -1;
-        f.l0[i] = f.l1[i] = 0.0f;
     }
+    for (size_t i = 0; i < npad; i++)
+        f.l0[i] = f.l1[i] = 0.0f;
     run_parallel(&f, out, 0, ntiles, P->threads);
     run_parallel(&f, out, 1, P->height, P->threads);
 

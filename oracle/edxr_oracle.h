@@ -45,6 +45,7 @@ typedef struct
     float light[3];   /* direction towards the light, normalised inside */
     float ks, shininess;
     int threads;      /* worker threads for the per-tile stages (>=1) */
+    int msaa_log2;    /* RenderStates::MultiSampleLevel: 0 (one sample) .. 5 (32 samples) */
 } edxr_oracle_params;
 
 typedef struct
@@ -57,10 +58,15 @@ typedef struct
     int nv, nt;
 } edxr_oracle_mesh;
 
+/* With S = 1 << msaa_log2 samples, id and depth hold S planes of W*H
+ * (sample s at offset s*W*H); the barycentrics are written for S == 1 only.
+ * colour is the winner's FP64 shading (S == 1) or the reference's resolve:
+ * each sample's winner shaded at the pixel centre and stored as 8 bits, the
+ * samples averaged in float (FrameBuffer::Resolve, FrameBuffer.cpp:70-87). */
 typedef struct
 {
-    uint32_t* id;     /* W*H input-triangle index of the winner, 0xFFFFFFFF if none */
-    float* depth;     /* W*H final depth buffer (clear value 1.0) */
+    uint32_t* id;     /* S*W*H input-triangle index of the winner, 0xFFFFFFFF if none */
+    float* depth;     /* S*W*H final depth buffer (clear value 1.0) */
     float* lambda0;   /* W*H winner barycentrics (optional) */
     float* lambda1;
     double* color;    /* W*H*4 RGBA, alpha 1 where covered (optional) */

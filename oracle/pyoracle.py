@@ -23,7 +23,7 @@ class _Params(ctypes.Structure):
                 ("depth_func", ctypes.c_int), ("hierarchical", ctypes.c_int),
                 ("shader", ctypes.c_int), ("light", ctypes.c_float * 3),
                 ("ks", ctypes.c_float), ("shininess", ctypes.c_float),
-                ("threads", ctypes.c_int)]
+                ("threads", ctypes.c_int), ("msaa_log2", ctypes.c_int)]
 
 
 class _Mesh(ctypes.Structure):
@@ -68,6 +68,8 @@ def reference_lib():
         fp, up, i = ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int
         _ref.edxr_ref_parity.argtypes = [i, i, fp, fp, fp, fp, i, up, i, i, up, fp, fp, fp]
         _ref.edxr_ref_parity.restype = ctypes.c_longlong
+        _ref.edxr_ref_parity_ms.argtypes = [i, i, fp, fp, fp, fp, i, up, i, i, i, up, fp]
+        _ref.edxr_ref_parity_ms.restype = ctypes.c_longlong
         _ref.edxr_ref_time.argtypes = [i, i, fp, fp, fp, fp, i, up, i, i, i, ctypes.POINTER(ctypes.c_int)]
         _ref.edxr_ref_time.restype = ctypes.c_double
     return _ref
@@ -77,7 +79,7 @@ def _ptr(a):
     return None if a is None else a.ctypes.data
 
 
-def make_params(view, threads=None, hierarchical=True, shader=None, depth_func=None):
+def make_params(view, threads=None, hierarchical=True, shader=None, depth_func=None, msaa_log2=0):
     p = _Params()
     p.width, p.height = view.width, view.height
     p.mv = _f16(*np.asarray(view.mv, np.float32).ravel())
@@ -89,12 +91,14 @@ def make_params(view, threads=None, hierarchical=True, shader=None, depth_func=N
     p.light = (ctypes.c_float * 3)(*np.asarray(view.light, np.float32))
     p.ks, p.shininess = view.ks, view.shininess
     p.threads = threads or os.cpu_count() or 1
+    p.msaa_log2 = msaa_log2
     return p
 
 
 def render_oracle(mesh, view, threads=None, hierarchical=True, depth_func=None, shader=None,
-                  with_color=True):
-    """Run the C restatement.  Returns a dict of numpy arrays and statistics."""
+                  with_color=True, msaa_log2=0):
+    """Run the C restatement.  Returns a dict of numpy arrays and statistics;
+    with msaa_log2 > 0, id and depth are (samples, H, W)."""
     lib = _oracle_lib()
     W, H = view.width, view.height
     pos = np.ascontiguousarray(mesh.positions, np.float32)
@@ -104,16 +108,20 @@ def render_oracle(mesh, view, threads=None, hierarchical=True, depth_func=None, 
     idx = np.ascontiguousarray(mesh.indices, np.uint32)
     m = _Mesh(pos.ctypes.data, 3, nrm.ctypes.data, 3, uv.ctypes.data, 2, alb.ctypes.data, 3,
               idx.ctypes.data, mesh.nv, mesh.nt)
-    out_id = np.empty((H, W), np.uint32)
-    out_depth = np.empty((H, W), np.float32)
+    S = 1 << msaa_log2
+    shape = (H, W) if S == 1 else (S, H, W)
+    out_id = np.empty(shape, np.uint32)
+    out_depth = np.empty(shape, np.float32)
     l0 = np.empty((H, W), np.float32)
     l1 = np.empty((H, W), np.float32)
     color = np.empty((H, W, 4), np.float64) if with_color else None
     o = _Out(out_id.ctypes.data, out_depth.ctypes.data, l0.ctypes.data, l1.ctypes.data, _ptr(color))
-    p = make_params(view, threads, hierarchical, shader, depth_func)
+    p = make_params(view, threads, hierarchical, shader, depth_func, msaa_log2)
     rc = lib.edxr_oracle_render(ctypes.byref(p), ctypes.byref(m), ctypes.byref(o))
     if rc != 0:
         raise RuntimeError("oracle failed with code %d" % rc)
+    if S > 1:
+        l0 = l1 = None
     return {"id": out_id, "depth": out_depth, "lambda0": l0, "lambda1": l1, "color": color,
             "fragments": o.fragments, "raster_tris": o.raster_tris,
             "clipped_input_tris": o.clipped_input_tris, "bin_refs": o.bin_refs}
@@ -152,6 +160,29 @@ def render_reference(mesh, view, hierarchical=True):
     if frags < 0:
         raise RuntimeError("reference harness rejected the arguments")
     return {"id": out_id, "depth": out_depth, "lambda0": l0, "lambda1": l1, "fragments": frags}
+
+
+def render_reference_ms(mesh, view, msaa_log2, hierarchical=True):
+    """The reference's own pipeline with 2^msaa_log2 samples per pixel
+    (Renderer::SetMSAAMode): per-sample winners and depths, (S, H, W)."""
+    lib = reference_lib()
+    if lib is None:
+        return None
+    W, H, S = view.width, view.height, 1 << msaa_log2
+    verts = mesh.interleaved_pnt()
+    idx = np.ascontiguousarray(mesh.indices, np.uint32)
+    mv = np.ascontiguousarray(view.mv, np.float32)
+    pr = np.ascontiguousarray(view.proj, np.float32)
+    ra = np.ascontiguousarray(view.raster, np.float32)
+    out_id = np.empty((S, H, W), np.uint32)
+    out_depth = np.empty((S, H, W), np.float32)
+    frags = lib.edxr_ref_parity_ms(W, H, mv.ctypes.data, pr.ctypes.data, ra.ctypes.data,
+                                   verts.ctypes.data, mesh.nv, idx.ctypes.data, mesh.nt,
+                                   1 if hierarchical else 0, msaa_log2, out_id.ctypes.data,
+                                   out_depth.ctypes.data)
+    if frags < 0:
+        raise RuntimeError("reference harness rejected the arguments")
+    return {"id": out_id, "depth": out_depth, "fragments": frags}
 
 
 def time_reference(mesh, view, frames=5, warmup=1):

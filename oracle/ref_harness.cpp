@@ -5,7 +5,7 @@
 // the C restatement in oracle/edxr_oracle.c and the timed CPU baseline.  It is
 // never linked into, or called by, the product library.
 //
-// Two entry points:
+// Entry points:
 //  * edxr_ref_parity  runs the reference stages in the order RenderMesh runs
 //    them (Renderer.cpp:100-118: Clear, VertexProcessing, Clipping,
 //    TiledRasterization) and reads back, per pixel, the fragment that the
@@ -14,6 +14,7 @@
 //    and the final tiled depth value (FrameBuffer.cpp:54-68).  Each input
 //    triangle i is given texture id i (Clipper.h:95, RasterTriangle.h:63,
 //    Shader.h:112), so the fragment carries the input-triangle index.
+//  * edxr_ref_parity_ms  the same with MSAA, per sample.
 //  * edxr_ref_time    times the public Renderer::RenderMesh end to end.
 #include "EDXPrerequisites.h"
 #include "Renderer.h"
@@ -183,6 +184,82 @@ long long edxr_ref_parity(int width, int height,
 				const FloatSSE& q = depth[ty * tileDimX + tx][Vector3i(0, ix >> 1, (Tile::SIZE - 1 - iy) >> 1)];
 				outDepth[(size_t)y * width + x] = q[(x & 1) + 2 * (y & 1)];
 			}
+	}
+	return fragments;
+}
+
+// The same with 2^msaaLog2 samples per pixel (Renderer::SetMSAAMode,
+// Renderer.cpp:94-98): per sample, the input-triangle id of the last fragment
+// in tile order whose coverage bit for that sample is set (UpdateFrameBuffer,
+// Renderer.cpp:305-350, bit (sId << 2) + lane) and the final tiled depth of
+// the sample.  Outputs are S planes of W*H, sample-major.
+long long edxr_ref_parity_ms(int width, int height,
+	const float* mv16, const float* proj16, const float* raster16,
+	const float* vertices, int nv, const uint32_t* indices, int nt,
+	int hierarchical, int msaaLog2,
+	uint32_t* outId, float* outDepth)
+{
+	if (width <= 0 || height <= 0 || nv < 0 || nt < 0 || msaaLog2 < 0 || msaaLog2 > 5)
+		return -1;
+
+	gPending.vertices = vertices;
+	gPending.nv = nv;
+	gPending.indices = indices;
+	gPending.nt = nt;
+	gPending.triangleIdAsTexture = true;
+
+	long long fragments = 0;
+	{
+		Renderer renderer;
+		SetupRenderer(renderer, width, height, mv16, proj16, raster16, hierarchical);
+		renderer.SetMSAAMode(msaaLog2);
+		Mesh mesh;
+		mesh.LoadMesh(Vector3(), Vector3(), Vector3(), "");
+
+		FrameBuffer* fb = (renderer.*Get(R_FrameBuffer())).Get();
+		const int S = (int)fb->GetSampleCount();
+		fb->Clear();
+		(renderer.*Get(R_VertexProcessing()))(mesh.GetVertexBuffer());
+		(renderer.*Get(R_Clipping()))(mesh.GetIndexBuffer(), mesh.GetTextureIds());
+		(renderer.*Get(R_TiledRasterization()))();
+
+		const size_t npix = (size_t)width * height;
+		for (size_t i = 0; i < npix * S; i++)
+			outId[i] = 0xFFFFFFFFu;
+
+		Array<Tile>& tiles = renderer.*Get(R_Tiles());
+		for (int t = 0; t < tiles.Size(); t++)
+		{
+			const Array<Fragment>& frags = tiles[t].fragmentBuf;
+			fragments += frags.Size();
+			for (int j = 0; j < frags.Size(); j++)
+			{
+				const Fragment& f = frags[j];
+				for (int s = 0; s < S; s++)
+					for (int lane = 0; lane < 4; lane++)
+					{
+						if (f.coverageMask.GetBit((s << 2) + lane) == 0)
+							continue;
+						const int x = f.x + (lane & 1);
+						const int y = f.y + (lane >> 1);
+						if (x >= width || y >= height)
+							continue;
+						outId[(size_t)s * npix + (size_t)y * width + x] = f.textureId;
+					}
+			}
+		}
+
+		Array<DimensionalArray<3, FloatSSE>>& depth = (*fb).*Get(FB_Depth());
+		const int tileDimX = (int)((*fb).*Get(FB_TileDimX()));
+		for (int s = 0; s < S; s++)
+			for (int y = 0; y < height; y++)
+				for (int x = 0; x < width; x++)
+				{
+					const int tx = x >> Tile::SIZE_LOG_2, ty = y >> Tile::SIZE_LOG_2;
+					const int ix = x & (Tile::SIZE - 1), iy = y & (Tile::SIZE - 1);
+					const FloatSSE& q = depth[ty * tileDimX + tx][Vector3i(s, ix >> 1, (Tile::SIZE - 1 - iy) >> 1)];
+					outDepth[(size_t)s * npix + (size_t)y * width + x] = q[(x & 1) + 2 * (y & 1)];
+				}
 	}
 	return fragments;
 }

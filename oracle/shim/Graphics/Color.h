@@ -14,7 +14,7 @@ namespace EDX
 	struct Color
 	{
 		float r, g, b, a;
-		Color(float v = 0.0f) : r(v), g(v), b(v), a(1.0f) {}
+		Color(float v = 0.0f) : r(v), g(v), b(v), a(v) {}
 		Color(float R, float G, float B, float A = 1.0f) : r(R), g(G), b(B), a(A) {}
 		inline Color(const Color4b& c);
 		Color& operator+=(const Color& o) { r += o.r; g += o.g; b += o.b; a += o.a; return *this; }

@@ -10,7 +10,7 @@ import pytest
 
 from edxraster_gb300 import scenes
 from oracle import pyoracle
-from _scenes import golden_names, load_golden, mismatch_report
+from _scenes import golden_names, load_golden, load_golden_ms, mismatch_report
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -23,6 +23,48 @@ def test_oracle_matches_golden(name):
     assert np.array_equal(o["lambda0"].view(np.uint32)[covered], exp["lambda0_bits"][covered])
     assert np.array_equal(o["lambda1"].view(np.uint32)[covered], exp["lambda1_bits"][covered])
     assert o["fragments"] == exp["fragments"]
+
+
+@pytest.mark.parametrize("name", golden_names(msaa=True))
+def test_oracle_matches_golden_msaa(name):
+    sc, hier, lg, exp = load_golden_ms(name)
+    o = pyoracle.render_oracle(sc.mesh, sc.view, hierarchical=hier, depth_func=scenes.DEPTH_LEQUAL, threads=2,
+                               msaa_log2=lg)
+    for s in range(1 << lg):
+        assert not mismatch_report("id[%d]" % s, o["id"][s], exp["id"][s])
+        assert not mismatch_report("depth[%d]" % s, o["depth"][s].view(np.uint32), exp["depth_bits"][s])
+    assert o["fragments"] == exp["fragments"]
+
+
+@pytest.mark.parametrize("lg", [1, 2, 3, 4, 5])
+def test_oracle_matches_reference_live_msaa(lg):
+    if pyoracle.reference_lib() is None:
+        pytest.skip("reference sources not available here")
+    sc = scenes.stress_scene(1500, 96, 72, seed=20 + lg, max_area=2e3)
+    r = pyoracle.render_reference_ms(sc.mesh, sc.view, lg)
+    o = pyoracle.render_oracle(sc.mesh, sc.view, depth_func=scenes.DEPTH_LEQUAL, threads=2, with_color=False,
+                               msaa_log2=lg)
+    assert np.array_equal(o["id"], r["id"])
+    assert np.array_equal(o["depth"].view(np.uint32), r["depth"].view(np.uint32))
+    assert o["fragments"] == r["fragments"]
+
+
+def test_msaa_resolve_arithmetic():
+    """The resolved colour of a pixel is the float average of its samples'
+    8-bit colours; a pixel whose samples all see one triangle resolves to
+    that triangle's 8-bit colour, and its alpha to 1."""
+    sc = scenes.sphere_scene(160, 96, slices=12, stacks=9)
+    one = pyoracle.render_oracle(sc.mesh, sc.view, threads=2)
+    four = pyoracle.render_oracle(sc.mesh, sc.view, threads=2, msaa_log2=2)
+    full = (four["id"] == one["id"][None]).all(axis=0) & (one["id"] != 0xFFFFFFFF)
+    assert full.sum() > 1000
+    q = np.floor(np.clip(one["color"][..., :3].astype(np.float32), 0, 1) * np.float32(255) + np.float32(0.5))
+    expect = (q / np.float32(255)).astype(np.float32)
+    # the float sum of four equal samples may round in its last bit
+    assert np.allclose(four["color"][..., :3][full], expect[full], rtol=0, atol=1e-6)
+    assert np.all(four["color"][..., 3][full] == 1.0)
+    empty = (four["id"] == 0xFFFFFFFF).all(axis=0)
+    assert np.all(four["color"][empty] == 0.0)
 
 
 def _live_cases():
