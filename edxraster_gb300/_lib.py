@@ -50,7 +50,7 @@ class Mesh(ctypes.Structure):
 
 class Outputs(ctypes.Structure):
     _fields_ = [("color", ctypes.c_void_p), ("depth", ctypes.c_void_p), ("triangle_id", ctypes.c_void_p),
-                ("width", ctypes.c_uint32), ("height", ctypes.c_uint32)]
+                ("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("samples", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):

@@ -170,7 +170,7 @@ struct edxr_renderer
     // the last pass, for synchronize / overflow recovery
     PassArgs last = {};
     bool pending = false;
-    uint32_t last_frames = 0, out_width = 0, out_height = 0;
+    uint32_t last_frames = 0, out_width = 0, out_height = 0, last_samples = 1;
     uint32_t rerenders = 0;
     uint8_t* back_host = nullptr;  // pinned, GetBackBuffer's RGBA8 copy
     size_t back_host_cap = 0;
@@ -353,8 +353,9 @@ void fill_frame(FrameDesc& f, const edxr_mesh& m, const Camera& cam, const Shadi
     }
 }
 
-// Build the pass over `n` frames (already in r->frames_host) and launch it.
-edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t height)
+// Build the pass over `n` frames (already in r->frames_host) and launch it,
+// with 2^msaa_log2 samples per pixel.
+edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t height, int msaa_log2 = 0)
 {
     uint64_t tv = 0, tt = 0, tiles = 0;
     for (uint32_t i = 0; i < n; i++)
@@ -403,9 +404,11 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     EDXR_CUDA(r->counters.ensure(4 * kCounters + 8 * std::max<uint64_t>(nscan, 1)));  // + scan status words
     EDXR_CUDA(r->status.ensure(sizeof(DeviceStatus)));
     EDXR_CUDA(r->color.ensure(16 * std::max<uint64_t>(pixels, 1)));
-    EDXR_CUDA(r->depth.ensure(4 * std::max<uint64_t>(pixels, 1)));
-    EDXR_CUDA(r->tri_id.ensure(4 * std::max<uint64_t>(pixels, 1)));
-    EDXR_CUDA(r->keybuf.ensure_zeroed(8 * std::max<uint64_t>(pixels, 1), r->stream));
+    // depth and triangle ids: one plane per sample
+    const uint64_t samples = 1ull << msaa_log2;
+    EDXR_CUDA(r->depth.ensure(4 * samples * std::max<uint64_t>(pixels, 1)));
+    EDXR_CUDA(r->tri_id.ensure(4 * samples * std::max<uint64_t>(pixels, 1)));
+    EDXR_CUDA(r->keybuf.ensure_zeroed(8 * samples * std::max<uint64_t>(pixels, 1), r->stream));
     const uint64_t icap = item_capacity(tiles, r->bin_capacity);
     EDXR_CUDA(r->items.ensure(sizeof(uint2) * icap));
 
@@ -443,6 +446,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.item_capacity = icap;
     a.keybuf = r->keybuf.as<unsigned long long>();
     a.total_pixels = pixels;
+    a.msaa_log2 = msaa_log2;
     a.num_sms = r->num_sms;
 
     EDXR_CUDA(run_pass(r, a));
@@ -451,6 +455,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     r->last = a;
     r->pending = true;
     r->last_frames = n;
+    r->last_samples = (uint32_t)samples;
     r->out_width = width;
     r->out_height = height;
     return EDXR_OK;
@@ -669,8 +674,8 @@ edxr_status edxr_set_state(edxr_renderer* r, const edxr_state* s)
         return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
     if (s->depth_func != EDXR_DEPTH_LEQUAL && s->depth_func != EDXR_DEPTH_LESS)
         return fail(EDXR_ERR_INVALID_ARG, "unknown depth function");
-    if (s->msaa_log2 != 0)
-        return fail(EDXR_ERR_UNSUPPORTED, "multisampling is not provided by this build (msaa_log2 must be 0)");
+    if (s->msaa_log2 < 0 || s->msaa_log2 > kMaxMsaaLog2)
+        return fail(EDXR_ERR_INVALID_ARG, "msaa_log2 must be in [0, 5] (1 to 32 samples)");
     r->state = *s;
     return EDXR_OK;
 }
@@ -715,7 +720,7 @@ edxr_status edxr_render(edxr_renderer* r, const edxr_mesh* mesh)
     cudaEventSynchronize(r->done);  // the pinned descriptor may still be in flight
     fill_frame(r->frames_host[0], dm, r->cam, r->shading, r->state.depth_func, r->state.hierarchical, r->width,
                r->height);
-    return launch_frames(r, 1, r->width, r->height);
+    return launch_frames(r, 1, r->width, r->height, r->state.msaa_log2);
 }
 
 edxr_status edxr_synchronize(edxr_renderer* r)
@@ -741,6 +746,7 @@ edxr_status edxr_get_outputs(edxr_renderer* r, edxr_outputs* out)
     out->triangle_id = r->tri_id.as<uint32_t>();
     out->width = r->out_width;
     out->height = r->out_height;
+    out->samples = r->last_samples;
     return EDXR_OK;
 }
 
@@ -755,9 +761,10 @@ edxr_status edxr_read_outputs(edxr_renderer* r, float* color, float* depth, uint
     if (!r->last_frames)
         return fail(EDXR_ERR_INVALID_ARG, "nothing rendered yet");
     const size_t n = (size_t)r->out_width * r->out_height;
+    const size_t ns = n * r->last_samples;  // depth and ids: one plane per sample
     if (color) EDXR_CUDA(cudaMemcpyAsync(color, r->color.ptr, 16 * n, cudaMemcpyDeviceToHost, r->stream));
-    if (depth) EDXR_CUDA(cudaMemcpyAsync(depth, r->depth.ptr, 4 * n, cudaMemcpyDeviceToHost, r->stream));
-    if (id) EDXR_CUDA(cudaMemcpyAsync(id, r->tri_id.ptr, 4 * n, cudaMemcpyDeviceToHost, r->stream));
+    if (depth) EDXR_CUDA(cudaMemcpyAsync(depth, r->depth.ptr, 4 * ns, cudaMemcpyDeviceToHost, r->stream));
+    if (id) EDXR_CUDA(cudaMemcpyAsync(id, r->tri_id.ptr, 4 * ns, cudaMemcpyDeviceToHost, r->stream));
     EDXR_CUDA(cudaStreamSynchronize(r->stream));
     return EDXR_OK;
 }
@@ -893,6 +900,8 @@ edxr_status edxr_render_batched(edxr_renderer* r, const edxr_mesh* meshes, uint3
         if (views[v].depth_func != EDXR_DEPTH_LEQUAL && views[v].depth_func != EDXR_DEPTH_LESS)
             return fail(EDXR_ERR_INVALID_ARG, "unknown depth function in view");
     }
+    if (r->state.msaa_log2 != 0)
+        return fail(EDXR_ERR_UNSUPPORTED, "the batched form renders one sample per pixel (set msaa_log2 to 0)");
     DeviceGuard g(r->device);
     if ((s = sync_pass(r)) != EDXR_OK)
         return s;
@@ -982,6 +991,8 @@ edxr_status diff_mesh(edxr_renderer* r, const edxr_mesh* mesh, const edxr_shader
         return s;
     if (!r->last_frames)
         return fail(EDXR_ERR_INVALID_ARG, "nothing rendered yet");
+    if (r->last_samples != 1)
+        return fail(EDXR_ERR_UNSUPPORTED, "the differentiable form takes a pass rendered with one sample per pixel");
     for (uint32_t i = 0; i < r->last_frames; i++)
         if (r->frames_host[i].nv != mesh->num_vertices || r->frames_host[i].nt != mesh->num_triangles)
             return fail(EDXR_ERR_INVALID_ARG, "mesh sizes differ from the mesh of the last pass");

@@ -150,8 +150,11 @@ struct PassArgs
     float* depth;
     uint32_t* tri_id;        // the winner's input-triangle id (kNoTriangle: background)
     uint64_t total_pixels;   // frames * width * height
+    int msaa_log2;           // samples per pixel = 1 << msaa_log2; depth and tri_id hold one plane per sample
     int num_sms;
 };
+
+constexpr int kMaxMsaaLog2 = 5;  // 32 samples (CoverageMask, Shader.h:52-54)
 
 // Host-side launchers (edxr_kernels.cu).
 constexpr int kStageEvents = 6;  // boundaries of the 5 timed stages

@@ -78,9 +78,12 @@ struct SmallTiles
 };
 
 // The tile range of a small triangle's entries and their number.
-__device__ __forceinline__ uint32_t small_tiles(const FrameDesc& f, const RTri& t, const BinGeom& g, SmallTiles& st)
+__device__ __forceinline__ uint32_t small_tiles(const PassArgs& a, const FrameDesc& f, const RTri& t, const BinGeom& g,
+                                               SmallTiles& st)
 {
-    const bool wf = wrap_free(t);
+    // with several samples per pixel a sample off the centre may be covered:
+    // keep the reference's quad-aligned region
+    const bool wf = a.msaa_log2 == 0 && wrap_free(t);
     const int x0 = max(wf ? g.cx0 : g.bbx0 & ~1, 0), x1 = min(wf ? g.cx1 : g.bbx1 | 1, f.width - 1);
     const int y0 = max(wf ? g.cy0 : g.bby0 & ~1, 0), y1 = min(wf ? g.cy1 : g.bby1 | 1, f.height - 1);
     if (x0 > x1 || y0 > y1)
@@ -231,7 +234,7 @@ __global__ void __launch_bounds__(256) k_setup(PassArgs a)
                     const BinGeom g = bin_geom(t, f);
                     big = !g.small;
                     if (g.small)
-                        nent = small_tiles(f, t, g, st);
+                        nent = small_tiles(a, f, t, g, st);
                 }
             }
             else
@@ -394,7 +397,7 @@ __global__ void __launch_bounds__(128) k_clip(PassArgs a)
             const BinGeom g = bin_geom(tk, f);
             bin_big_append(a, out, !g.small);
             SmallTiles st;
-            const uint32_t nent = g.small ? small_tiles(f, tk, g, st) : 0u;
+            const uint32_t nent = g.small ? small_tiles(a, f, tk, g, st) : 0u;
             if (nent)
                 bin_small(a, f, out, st, atomicAdd(&a.counters[5], nent));
             out++;
@@ -780,9 +783,13 @@ __device__ __forceinline__ uint32_t zmin_key(const RTri& t, bool wf)
 
 // Tile-relative edge equations, barycentric numerators and region of one
 // bin entry.
+// With MS (several samples per pixel) it also returns G[k] = B[k] + C[k]:
+// sample s sits at (o, o) from the pixel centre (see kSampleOffsets), where
+// edge k changes by o * G[k]; and it keeps the quad-aligned region.
+template <bool MS = false>
 __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uint32_t nr, uint32_t rank_base,
                                           int tileX, int tileY,
-                                          StagedTri& s, uint32_t& zkey)
+                                          StagedTri& s, uint32_t& zkey, int* G = nullptr)
 {
     const uint32_t ri = entry >> 2;
     if (ri >= nr)
@@ -812,7 +819,13 @@ __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uin
     // and 2 measured from v2, equal to the unbiased edge values
     s.A1 = A[1]; s.D1 = D[1]; s.K1 = K[1];
     s.A2 = A[2]; s.D2 = D[2]; s.K2 = K[2];
-    const bool wf = wrap_free(t);
+    if (MS)
+    {
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            G[k] = wadd(e.B[k], e.C[k]);
+    }
+    const bool wf = !MS && wrap_free(t);
     int lx0 = 0, lx1 = 15, ly0 = 0, ly1 = 15;
     if (!accept)
     {
@@ -1137,6 +1150,274 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
 }
 
 // -------------------------------------------------------------------------
+// Multisampling (Renderer::SetMSAAMode, Renderer.cpp:94-98).
+//
+// FrameBuffer::MultiSampleOffsets (FrameBuffer.cpp:107-191): the reference's
+// table of 1/16-pixel sample offsets per sample-count log2.  Its rasterizer
+// reads sample s as `const Vector2i& sampleOffset = MultiSampleOffsets[level]
+// [2 * s]` (Rasterizer.h:247, 382): the int goes through Vector2i's scalar
+// constructor, so the sample sits at (o, o) with o = table[level][2 s].
+__constant__ int kSampleOffsets[kMaxMsaaLog2 + 1][64] = {
+    { 0, 0 },
+    { 4, 4, -4, -4 },
+    { -2, -6, 6, -2, -6, 2, 2, 6 },
+    { 1, -3, -1, 3, 5, 1, -3, -5, -5, 5, -7, -1, 3, 7, 7, -7 },
+    { 1, 1, -1, -3, -3, 2, 4, -1, -5, -2, 2, 5, 5, 3, 3, -5,
+      -2, 6, 0, -7, -4, -6, -6, 4, -8, 0, 7, -4, 6, 7, -7, -8 },
+    { 1, 1, -1, -3, -3, 2, 4, -1, -5, -2, 2, 5, 5, 3, 3, -5,
+      -2, 6, 0, -7, -4, -6, -6, 4, -8, 0, 7, -4, 6, 7, -7, -8,
+      1, 3, -3, -3, -3, 0, 6, -2, -7, -1, 3, 4, 7, 3, 3, -6,
+      -2, 7, 0, -4, -2, -5, -7, 6, -8, 3, 4, -1, 2, 7, 4, -8 }
+};
+
+__device__ __forceinline__ int sample_offset(int level, int s) { return kSampleOffsets[level][2 * s]; }
+
+// Key of sample s (offset o) of staged triangle st at tile pixel (lx, ly):
+// FineRasterize_MultiSample / TrivialAcceptTriangle_MultiSample
+// (Rasterizer.h:202-300, 355-415): the biased pixel-centre edge values plus
+// o * G decide coverage (accepted entries skip the test), the barycentrics
+// and depth come from the unbiased values at the sample.
+__device__ __forceinline__ bool sample_key(const StagedTri& st, const int* G, int lx, int ly, int o, bool less,
+                                           uint64_t& key)
+{
+    const uint32_t fl = st.flags;
+    const int l1 = wadd(wadd(wadd(wmul(st.A1, lx), wmul(st.D1, ly)), st.K1), wmul(o, G[1]));
+    const int l2 = wadd(wadd(wadd(wmul(st.A2, lx), wmul(st.D2, ly)), st.K2), wmul(o, G[2]));
+    if (!(fl & (1u << 20)))
+    {
+        const int e0 = wadd(wadd(wadd(wmul(st.A0, lx), wmul(st.D0, ly)), st.K0), wmul(o, G[0]));
+        const int e1 = wadd(l1, (fl & (1u << 21)) ? -1 : 0);
+        const int e2 = wadd(l2, (fl & (1u << 22)) ? -1 : 0);
+        if ((e0 | e1 | e2) < 0)
+            return false;
+    }
+    const float L0 = fmul(__int2float_rn(l1), st.invDet);
+    const float L1 = fmul(__int2float_rn(l2), st.invDet);
+    const float L2 = fsub(fsub(1.0f, L0), L1);
+    const float d = fadd(fadd(fmul(L0, st.z0), fmul(L1, st.z1)), fmul(L2, st.z2));
+    if (d != d)
+        return false;
+    key = ((uint64_t)depth_key(d) << 32) | (less ? st.rank : ~st.rank);
+    return true;
+}
+
+// Float -> 8 bits as Color4b::FromFloats: clamp, scale by 255, round half up.
+__device__ __forceinline__ uint32_t to_byte(float v)
+{
+    v = fminf(fmaxf(v, 0.0f), 1.0f);
+    return (uint32_t)fadd(fmul(v, 255.0f), 0.5f);
+}
+
+// Depth of raster triangle t at 1/16-pixel position (x, y)
+// (RasterTriangle.h:324-337).
+__device__ __forceinline__ float depth_at(const RTri& t, int x, int y, float& L0, float& L1)
+{
+    const Edges e = tri_edges(t);
+    const int n1 = wadd(wmul(e.B[1], wsub(x, t.v2x)), wmul(e.C[1], wsub(y, t.v2y)));
+    const int n2 = wadd(wmul(e.B[2], wsub(x, t.v2x)), wmul(e.C[2], wsub(y, t.v2y)));
+    L0 = fmul(__int2float_rn(n1), t.invDet);
+    L1 = fmul(__int2float_rn(n2), t.invDet);
+    const float L2 = fsub(fsub(1.0f, L0), L1);
+    return fadd(fadd(fmul(L0, t.z0), fmul(L1, t.z1)), fmul(L2, t.z2));
+}
+
+// The output of one pixel with S samples: per sample the winner's id and its
+// depth at the sample; the colour is the reference's resolve
+// (FrameBuffer::Resolve, FrameBuffer.cpp:70-87): each sample stores its
+// winner's colour shaded at the pixel centre as 8 bits (Renderer.cpp:
+// 295-350), the samples are averaged in float (alpha 1 per covered sample,
+// 0 for the clear value).  Samples that share a winner share its shading.
+static __device__ __noinline__ void write_pixel_ms(const PassArgs& a, const FrameDesc& f, const uint32_t* ri, int S,
+                                                   uint64_t pix, int px, int py)
+{
+    const int level = a.msaa_log2;
+    const uint64_t plane = a.total_pixels;
+    float acc[4] = { 0.f, 0.f, 0.f, 0.f };
+    uint32_t last = kNoTriangle, c8[3] = { 0u, 0u, 0u };
+    for (int s = 0; s < S; s++)
+    {
+        const uint32_t r = ri[s];
+        if (r == kNoTriangle)
+        {
+            a.depth[s * plane + pix] = 1.0f;
+            a.tri_id[s * plane + pix] = kNoTriangle;
+            continue;
+        }
+        const RTri t = a.rtris[r];
+        const int o = sample_offset(level, s);
+        float L0, L1;
+        a.depth[s * plane + pix] = depth_at(t, (px << 4) + 8 + o, (py << 4) + 8 + o, L0, L1);
+        a.tri_id[s * plane + pix] = t.order >> 4;
+        if (r != last)
+        {
+            depth_at(t, (px << 4) + 8, (py << 4) + 8, L0, L1);
+            const float3 c = shade_fragment(f, t, a.polys, L0, L1);
+            c8[0] = to_byte(c.x);
+            c8[1] = to_byte(c.y);
+            c8[2] = to_byte(c.z);
+            last = r;
+        }
+#pragma unroll
+        for (int q = 0; q < 3; q++)
+            acc[q] = fadd(acc[q], fdiv((float)c8[q], 255.0f));
+        acc[3] = fadd(acc[3], 1.0f);
+    }
+    const float inv = fdiv(1.0f, (float)S);
+    a.color[pix] = make_float4(fmul(acc[0], inv), fmul(acc[1], inv), fmul(acc[2], inv), fmul(acc[3], inv));
+}
+
+// Raster with S samples per pixel: persistent warps on the same work items
+// as k_raster, keys [sample][pixel] in dynamic shared memory, every entry
+// rasterized pixel-parallel with a loop over the samples.  Split tiles merge
+// per sample in the key buffer (S planes).
+constexpr int kMsRegionCap = 256;
+
+template <int S>
+__global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
+{
+    extern __shared__ unsigned long long ms_shared[];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long* key = ms_shared + (size_t)warp * (256 * S + 32 * 10);
+    StagedTri* staged = reinterpret_cast<StagedTri*>(key + 256 * S);            // 32 x 64 bytes
+    int* sg = reinterpret_cast<int*>(key + 256 * S + 32 * 8);                    // 32 x 3 ints (G)
+    const int level = a.msaa_log2;
+    const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
+    const uint32_t nheavy = *(volatile uint32_t*)&a.counters[6];
+    const uint32_t nitems = (uint32_t)min((uint64_t)nheavy + *(volatile uint32_t*)&a.counters[7], a.item_capacity);
+    const uint64_t plane = a.total_pixels;
+    for (;;)
+    {
+        uint32_t q = 0;
+        if (lane == 0)
+            q = atomicAdd(&a.counters[3], 1u);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= nitems)
+            break;
+        const uint2 item = a.items[q < nheavy ? q : (uint32_t)(a.item_capacity - 1 - (q - nheavy))];
+        const uint32_t tile = item.x;
+        const uint32_t fi = find_frame(a.frames, a.num_frames, tile, [](const FrameDesc& f) { return f.tile_base; });
+        const FrameDesc& f = a.frames[fi];
+        const uint32_t lt = tile - f.tile_base;
+        const int tileX = (int)(lt % (uint32_t)f.tdx), tileY = (int)(lt / (uint32_t)f.tdx);
+        const bool less = f.depth_func == 1;
+        uint32_t count = a.tile_count[tile];
+        const uint32_t start = a.tile_offset[tile];
+        if ((uint64_t)start + count > a.bin_capacity)
+            count = 0;  // overflowed frame: rendered again by the host
+        const uint32_t e0 = start + item.y * kItemEntries;
+        const uint32_t e1 = min(start + count, e0 + kItemEntries);
+        const unsigned long long clear = ((unsigned long long)0xBF800000u << 32) | (less ? 0u : 0xFFFFFFFFu);
+        for (int k = (int)lane; k < 256 * S; k += 32)
+            key[k] = clear;
+        __syncwarp();
+
+        for (uint32_t c = e0; c < e1; c += 32)
+        {
+            const uint32_t m = min(32u, e1 - c);
+            bool live = false;
+            if (lane < m)
+            {
+                StagedTri st;
+                uint32_t zk;
+                int G[3];
+                stage_tri<true>(a, a.bins[c + lane], nr, f.tri_base << 4, tileX, tileY, st, zk, G);
+                const uint32_t fl = st.flags;
+                live = (fl & 31) <= ((fl >> 5) & 31) && ((fl >> 10) & 31) <= ((fl >> 15) & 31);
+                staged[lane] = st;
+                sg[3 * lane] = G[0];
+                sg[3 * lane + 1] = G[1];
+                sg[3 * lane + 2] = G[2];
+            }
+            uint32_t todo = __ballot_sync(0xffffffffu, live);
+            __syncwarp();
+            while (todo)
+            {
+                const int j = __ffs(todo) - 1;
+                todo &= todo - 1u;
+                const StagedTri st = staged[j];
+                const int G[3] = { sg[3 * j], sg[3 * j + 1], sg[3 * j + 2] };
+                const uint32_t fl = st.flags;
+                const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31, ry1 = (fl >> 15) & 31;
+                const int rw = rx1 - rx0 + 1, area = rw * (ry1 - ry0 + 1);
+                for (int p = (int)lane; p < area; p += 32)
+                {
+                    const int dy = p / rw;
+                    const int x = rx0 + p - dy * rw, y = ry0 + dy;
+#pragma unroll 4
+                    for (int s = 0; s < S; s++)
+                    {
+                        uint64_t k;
+                        unsigned long long& slot = key[s * 256 + y * 16 + x];
+                        if (sample_key(st, G, x, y, sample_offset(level, s), less, k) && k < slot)
+                            slot = k;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+
+        bool shade = true;
+        if (count > kItemEntries)
+        {
+            for (int k = (int)lane; k < 256 * S; k += 32)
+            {
+                const int s = k >> 8, p = k & 255;
+                const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
+                const unsigned long long kk = key[k];
+                if (px < f.width && py < f.height && kk < clear)
+                    atomicMax(&a.keybuf[s * plane + f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px], ~kk);
+            }
+            __threadfence();
+            __syncwarp();
+            uint32_t left = 0;
+            if (lane == 0)
+                left = atomicSub(&a.tile_cursor[tile], e1 - e0) - (e1 - e0);
+            shade = __shfl_sync(0xffffffffu, left, 0) == 0;
+            if (shade)
+            {
+                __threadfence();
+                for (int k = (int)lane; k < 256 * S; k += 32)
+                {
+                    const int s = k >> 8, p = k & 255;
+                    const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
+                    if (px < f.width && py < f.height)
+                    {
+                        const unsigned long long m = atomicExch(
+                            &a.keybuf[s * plane + f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px], 0ull);
+                        key[k] = m ? ~m : clear;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        if (shade)
+        {
+#pragma unroll 1
+            for (int k = 0; k < 8; k++)
+            {
+                const int p = (int)lane + 32 * k;
+                const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
+                if (px >= f.width || py >= f.height)
+                    continue;
+                uint32_t ri[S];
+#pragma unroll
+                for (int s = 0; s < S; s++)
+                {
+                    const uint32_t low = (uint32_t)key[s * 256 + p];
+                    ri[s] = raster_triangle_of(a, less ? low : ~low, nr);
+                }
+                write_pixel_ms(a, f, ri, S, f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px, px, py);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Warps per block and dynamic shared memory of k_raster_ms with S samples.
+static int ms_warps(int S) { return S <= 8 ? 4 : (S == 16 ? 2 : 1); }
+static size_t ms_smem(int S) { return (size_t)ms_warps(S) * (256 * S + 32 * 10) * sizeof(unsigned long long); }
+
+// -------------------------------------------------------------------------
 // Renderer::GetBackBuffer compatibility: RGBA8, bottom-up (FrameBuffer.cpp:41).
 __global__ void k_back_buffer(const float4* color, uchar4* out, int width, int height)
 {
@@ -1145,16 +1426,13 @@ __global__ void k_back_buffer(const float4* color, uchar4* out, int width, int h
         return;
     const int x = i % width, y = i / width;
     const float4 c = color[i];
-    auto b = [](float v) -> unsigned char {
-        v = fminf(fmaxf(v, 0.0f), 1.0f);
-        return (unsigned char)(v * 255.0f + 0.5f);
-    };
-    const bool covered = c.w > 0.0f;
-    out[(size_t)(height - 1 - y) * width + x] = make_uchar4(b(c.x), b(c.y), b(c.z), covered ? 255 : 0);
+    // Color4b::FromFloats for one sample (alpha 1 or 0), Color4b(Color) of
+    // the resolve with several (alpha = covered share)
+    out[(size_t)(height - 1 - y) * width + x] =
+        make_uchar4(to_byte(c.x), to_byte(c.y), to_byte(c.z), to_byte(c.w));
 }
 
 // -------------------------------------------------------------------------
-
 
 // Raster variants: 0 and 1 carry the triangle-parallel path (no register cap /
 // capped for 5 blocks per SM); 2 is pixel-parallel only, capped for 6.
@@ -1185,11 +1463,45 @@ static int raster_blocks(int sms, const Tuning& t)
     return sms * per;
 }
 
+// Resident blocks per SM of k_raster_ms with 2^level samples (the dynamic
+// shared-memory limit raised first).
+template <int S>
+static int ms_occupancy_of()
+{
+    int n = 0;
+    if (cudaFuncSetAttribute(k_raster_ms<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ms_smem(S)) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster_ms<S>, 32 * ms_warps(S), ms_smem(S)) !=
+            cudaSuccess ||
+        n < 1)
+        n = 1;
+    return n;
+}
+
+static int ms_occupancy(int level)
+{
+    static int per_sm[kMaxMsaaLog2 + 1] = {};
+    if (!per_sm[level])
+    {
+        switch (level)
+        {
+        case 1: per_sm[1] = ms_occupancy_of<2>(); break;
+        case 2: per_sm[2] = ms_occupancy_of<4>(); break;
+        case 3: per_sm[3] = ms_occupancy_of<8>(); break;
+        case 4: per_sm[4] = ms_occupancy_of<16>(); break;
+        default: per_sm[5] = ms_occupancy_of<32>(); break;
+        }
+    }
+    return per_sm[level];
+}
+
 void prepare_kernels()
 {
     raster_occupancy(0);
     raster_occupancy(1);
     raster_occupancy(2);
+    for (int level = 1; level <= kMaxMsaaLog2; level++)
+        ms_occupancy(level);
 }
 
 Tuning default_tuning()
@@ -1223,7 +1535,20 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
     mark(3);
     k_bin_move<<<sms * (a.tune.bin_blocks_per_sm > 0 ? a.tune.bin_blocks_per_sm : 8), 256, 0, s>>>(a);
     mark(4);
-    if (a.tune.raster_variant == 2)
+    if (a.msaa_log2 > 0)
+    {
+        const int level = min(a.msaa_log2, kMaxMsaaLog2), S = 1 << level;
+        const int blocks = sms * ms_occupancy(level), threads = 32 * ms_warps(S);
+        switch (level)
+        {
+        case 1: k_raster_ms<2><<<blocks, threads, ms_smem(2), s>>>(a); break;
+        case 2: k_raster_ms<4><<<blocks, threads, ms_smem(4), s>>>(a); break;
+        case 3: k_raster_ms<8><<<blocks, threads, ms_smem(8), s>>>(a); break;
+        case 4: k_raster_ms<16><<<blocks, threads, ms_smem(16), s>>>(a); break;
+        default: k_raster_ms<32><<<blocks, threads, ms_smem(32), s>>>(a); break;
+        }
+    }
+    else if (a.tune.raster_variant == 2)
         k_raster<6, false><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
     else if (a.tune.raster_variant == 1)
         k_raster<5, true><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);

@@ -167,12 +167,19 @@ class Renderer:
                                                 ctypes.addressof(self._raster)))
 
     def SetMSAAMode(self, msaa_count_log2: int):
-        """Renderer::SetMSAAMode (Renderer.cpp:94-98); only 0 is provided."""
+        """Renderer::SetMSAAMode (Renderer.cpp:94-98): 2^msaa_count_log2 samples
+        per pixel, 0..5 (1 to 32 samples)."""
+        old = self._state.msaa_log2
         self._state.msaa_log2 = msaa_count_log2
         try:
             _lib.check(self._lib.edxr_set_state(self._h, ctypes.byref(self._state)))
-        finally:
-            self._state.msaa_log2 = 0
+        except Exception:
+            self._state.msaa_log2 = old
+            raise
+
+    @property
+    def samples(self) -> int:
+        return 1 << self._state.msaa_log2
 
     def SetTextureFilter(self, texture_filter: int):
         """Renderer::SetTextureFilter (Renderer.h:48); stored, no texture sampling here."""
@@ -239,11 +246,14 @@ class Renderer:
 
     # -- outputs -------------------------------------------------------------
     def ReadOutputs(self):
-        """Host copies of the last frame: colour (H,W,4) f32, depth (H,W) f32, triangle id (H,W) u32."""
+        """Host copies of the last frame: colour (H,W,4) f32, depth (H,W) f32, triangle id (H,W) u32;
+        with several samples per pixel depth and id are (S,H,W) and colour is the resolve."""
         W, H = self._width, self._height
+        o = self.DeviceOutputs()
+        shape = (H, W) if o.samples <= 1 else (o.samples, H, W)
         color = np.empty((H, W, 4), np.float32)
-        depth = np.empty((H, W), np.float32)
-        tid = np.empty((H, W), np.uint32)
+        depth = np.empty(shape, np.float32)
+        tid = np.empty(shape, np.uint32)
         _lib.check(self._lib.edxr_read_outputs(self._h, color.ctypes.data, depth.ctypes.data, tid.ctypes.data))
         return color, depth, tid
 

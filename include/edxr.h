@@ -99,7 +99,7 @@ typedef struct edxr_state
 {
     int depth_func;          /* edxr_depth_func                              */
     int hierarchical;        /* RenderStates::HierarchicalRasterize (1)      */
-    int msaa_log2;           /* RenderStates::MultiSampleLevel; must be 0    */
+    int msaa_log2;           /* RenderStates::MultiSampleLevel: 0..5 = 1..32 samples */
     int texture_filter;      /* RenderStates::TexFilter; stored only         */
 } edxr_state;
 
@@ -127,13 +127,19 @@ typedef struct edxr_mesh
     int memory;                                      /* edxr_memory    */
 } edxr_mesh;
 
-/* Renderer-owned device buffers, valid until the next render or resize. */
+/* Renderer-owned device buffers, valid until the next render or resize.
+ * With S = 2^msaa_log2 samples per pixel, depth and triangle_id hold S
+ * planes of width*height (sample s at offset s*width*height) and colour is
+ * the reference's resolve (FrameBuffer::Resolve, FrameBuffer.cpp:70-87): the
+ * samples' 8-bit colours (each shaded at the pixel centre) averaged in
+ * float, alpha = covered samples / S. */
 typedef struct edxr_outputs
 {
     float* color;            /* width*height*4 RGBA32F, row 0 = top; alpha 1 where covered */
-    float* depth;            /* width*height D32F, cleared to 1.0                          */
-    uint32_t* triangle_id;   /* width*height input-triangle index, 0xFFFFFFFF = none        */
+    float* depth;            /* S*width*height D32F, cleared to 1.0                        */
+    uint32_t* triangle_id;   /* S*width*height input-triangle index, 0xFFFFFFFF = none      */
     uint32_t width, height;
+    uint32_t samples;        /* S                                                          */
 } edxr_outputs;
 
 typedef struct edxr_stats
@@ -159,7 +165,12 @@ edxr_status edxr_set_transform(edxr_renderer* r, const float mv[16], const float
                                const float raster[16]);
 
 /* RenderStates fields (RenderStates.h:15-28) and the setters of Renderer.h:47-49
- * (SetMSAAMode, SetTextureFilter, SetHierarchicalRasterize). */
+ * (SetMSAAMode, SetTextureFilter, SetHierarchicalRasterize).  With
+ * msaa_log2 > 0 (Renderer::SetMSAAMode, Renderer.cpp:94-98) edxr_render
+ * rasterizes 2^msaa_log2 samples per pixel (FineRasterize_MultiSample /
+ * TrivialAcceptTriangle_MultiSample, Rasterizer.h:202-300, 355-415); the
+ * batched and differentiable forms and edxr_render_noalloc take one sample
+ * per pixel and return EDXR_ERR_UNSUPPORTED otherwise. */
 edxr_status edxr_set_state(edxr_renderer* r, const edxr_state* state);
 
 /* Shader selection (the reference hard-wires it in Renderer::Initialize,

@@ -191,7 +191,7 @@ public:
         edxr::Check(edxr_get_back_buffer(mpRenderer, &p));
         return p;
     }
-    // Renderer::SetMSAAMode (Renderer.cpp:94-98); only 0 is provided.
+    // Renderer::SetMSAAMode (Renderer.cpp:94-98): 2^msaaCountLog2 samples per pixel (0..5).
     void SetMSAAMode(int msaaCountLog2)
     {
         edxr_state s = mState;

@@ -58,11 +58,11 @@ int main(int argc, char** argv)
         bool threw = false;
         try
         {
-            renderer.SetMSAAMode(2);  // not provided: must throw, renderer stays usable
+            renderer.SetMSAAMode(6);  // at most 32 samples: must throw, renderer stays usable
         }
         catch (const edxr::Error& e)
         {
-            threw = e.status == EDXR_ERR_UNSUPPORTED;
+            threw = e.status == EDXR_ERR_INVALID_ARG;
         }
         if (!threw)
             return 4;

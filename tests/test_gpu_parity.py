@@ -154,6 +154,6 @@ def test_invalid_arguments_raise(cuda_lib):
     with pytest.raises(R.EdxrError):
         r.RenderMesh(bad)
     with pytest.raises(R.EdxrError):
-        r.SetMSAAMode(2)
+        r.SetMSAAMode(6)  # at most 32 samples
     r.RenderMesh(sc.mesh)  # the renderer is still usable
     r.close()
