@@ -239,7 +239,7 @@ def apply_tuning(r, workload):
     return t
 
 
-def measure_plain(sc, device, steps, warmup, flush_l2, workload=None):
+def measure_plain(sc, device, steps, warmup, flush_l2, workload=None, msaa_log2=0):
     import torch
     from edxraster_gb300 import renderer as R
     stream = torch.cuda.Stream()
@@ -248,6 +248,8 @@ def measure_plain(sc, device, steps, warmup, flush_l2, workload=None):
     R.configure(r, sc.view)
     if workload:
         apply_tuning(r, workload)
+    if msaa_log2:
+        r.SetMSAAMode(msaa_log2)
     dm = R.DeviceMesh.from_mesh(sc.mesh, device="cuda:%d" % device)
     ms = time_frames(r, stream, lambda: flush_l2(stream), lambda: r.RenderMesh(dm, synchronize=False),
                      steps, warmup) / steps
@@ -531,6 +533,10 @@ def run_gpu(args, world, rank, local):
             if wname != args.workload:
                 per_config[wname] = measure_plain(WORKLOADS[wname][1](), local, max(3, args.steps // 4), 3, flush_on,
                                                   workload=wname)
+        # Renderer::SetMSAAMode: 4 and 8 samples per pixel
+        for wname, lg in (("sphere", 2), ("terrain", 2), ("terrain", 3)):
+            per_config["%s_msaa%d" % (wname, 1 << lg)] = measure_plain(
+                WORKLOADS[wname][1](), local, max(3, args.steps // 4), 3, flush_on, workload=wname, msaa_log2=lg)
         per_config["batched"] = measure_batched(local, 3, 3, flush_on)
         per_config["differentiable"] = measure_diff(local, 5, 3)
 
