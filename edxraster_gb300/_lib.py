@@ -45,7 +45,13 @@ class Mesh(ctypes.Structure):
                 ("uvs", ctypes.c_void_p), ("uv_stride", ctypes.c_uint32),
                 ("albedo", ctypes.c_void_p), ("albedo_stride", ctypes.c_uint32),
                 ("indices", ctypes.c_void_p), ("num_vertices", ctypes.c_uint32),
-                ("num_triangles", ctypes.c_uint32), ("memory", ctypes.c_int)]
+                ("num_triangles", ctypes.c_uint32), ("memory", ctypes.c_int),
+                ("texture_ids", ctypes.c_void_p)]
+
+
+class Texture(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("format", ctypes.c_int),
+                ("texels", ctypes.c_void_p)]
 
 
 class Outputs(ctypes.Structure):
@@ -90,6 +96,7 @@ SIGNATURES = {
     "edxr_set_state": ([_P, ctypes.POINTER(State)], ctypes.c_int),
     "edxr_set_shader": ([_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ShaderParams)], ctypes.c_int),
     "edxr_render": ([_P, ctypes.POINTER(Mesh)], ctypes.c_int),
+    "edxr_set_textures": ([_P, ctypes.POINTER(Texture), ctypes.c_uint32], ctypes.c_int),
     "edxr_synchronize": ([_P], ctypes.c_int),
     "edxr_get_outputs": ([_P, ctypes.POINTER(Outputs)], ctypes.c_int),
     "edxr_read_outputs": ([_P, _P, _P, _P], ctypes.c_int),

@@ -141,7 +141,7 @@ struct Shading
 
 struct MeshStage
 {
-    DevBuf pos, nrm, alb, idx;
+    DevBuf pos, nrm, alb, uv, tid, idx;
 };
 
 }  // namespace
@@ -159,6 +159,9 @@ struct edxr_renderer
     DevBuf frames, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, bins, bin_tmp, big_list, counters,
         status;
     DevBuf color, depth, tri_id, back8, diff_scratch, tri_first, items, keybuf;
+    // texture slots (edxr_set_textures): descriptors and the texel pool with mip chains
+    DevBuf tex_desc, tex_texels;
+    uint32_t num_textures = 0;
     uint64_t bin_capacity = 0, rtri_cap = 0, poly_cap = 0, big_cap = 0;
     uint64_t debug_cap = 0;  // EDXR_DEBUG_CAPACITY: tiny starting capacities (tests)
     std::vector<MeshStage> stage;
@@ -261,7 +264,9 @@ edxr_status check_mesh(const edxr_mesh* m)
 }
 
 // Copy a host mesh to device staging buffers; returns a device-memory mesh.
-edxr_status stage_mesh(edxr_renderer* r, size_t slot, const edxr_mesh* in, edxr_mesh* out)
+// Texture coordinates and texture ids are uploaded only for the textured
+// shader, the one that samples them.
+edxr_status stage_mesh(edxr_renderer* r, size_t slot, const edxr_mesh* in, edxr_mesh* out, bool textured = false)
 {
     *out = *in;
     if (in->memory == EDXR_MEMORY_DEVICE)
@@ -284,9 +289,24 @@ edxr_status stage_mesh(edxr_renderer* r, size_t slot, const edxr_mesh* in, edxr_
     if ((st = copy(s.pos, in->positions, in->position_stride, 12, &out->positions, &out->position_stride))) return st;
     if ((st = copy(s.nrm, in->normals, in->normal_stride, 12, &out->normals, &out->normal_stride))) return st;
     if ((st = copy(s.alb, in->albedo, in->albedo_stride, 12, &out->albedo, &out->albedo_stride))) return st;
-    // no kernel samples texture coordinates, so they are not uploaded
-    out->uvs = nullptr;
-    out->uv_stride = 0;
+    if (textured)
+    {
+        if ((st = copy(s.uv, in->uvs, in->uv_stride, 8, &out->uvs, &out->uv_stride))) return st;
+        if (in->texture_ids)
+        {
+            const size_t tb = 4ull * in->num_triangles;
+            EDXR_CUDA(s.tid.ensure(tb > 0 ? tb : 16));
+            if (tb)
+                EDXR_CUDA(cudaMemcpyAsync(s.tid.ptr, in->texture_ids, tb, cudaMemcpyHostToDevice, r->stream));
+            out->texture_ids = s.tid.as<uint32_t>();
+        }
+    }
+    else
+    {
+        out->uvs = nullptr;
+        out->uv_stride = 0;
+        out->texture_ids = nullptr;
+    }
     const size_t ib = 12ull * in->num_triangles;
     EDXR_CUDA(s.idx.ensure(ib > 0 ? ib : 16));
     if (ib)
@@ -297,9 +317,14 @@ edxr_status stage_mesh(edxr_renderer* r, size_t slot, const edxr_mesh* in, edxr_
 }
 
 void fill_frame(FrameDesc& f, const edxr_mesh& m, const Camera& cam, const Shading& sh, int depth_func,
-                int hierarchical, uint32_t width, uint32_t height)
+                int hierarchical, uint32_t width, uint32_t height, const edxr_renderer* r)
 {
     std::memset(&f, 0, sizeof(f));
+    f.tex_ids = m.texture_ids;
+    f.textures = r->tex_desc.as<TexDesc>();
+    f.texels = r->tex_texels.as<float4>();
+    f.num_textures = r->num_textures;
+    f.tex_filter = r->state.texture_filter;
     f.positions = static_cast<const char*>(m.positions);
     f.normals = static_cast<const char*>(m.normals);
     f.albedo = static_cast<const char*>(m.albedo);
@@ -620,12 +645,12 @@ edxr_status edxr_destroy(edxr_renderer* r)
     DevBuf* bufs[] = { &r->frames, &r->rtris, &r->polys, &r->clip_list, &r->tile_count, &r->tile_offset,
                        &r->tile_cursor, &r->bins, &r->bin_tmp, &r->big_list, &r->counters, &r->status, &r->color,
                        &r->depth, &r->tri_id, &r->back8, &r->diff_scratch, &r->tri_first, &r->items,
-                       &r->keybuf };
+                       &r->keybuf, &r->tex_desc, &r->tex_texels };
     for (DevBuf* b : bufs)
         b->release();
     for (auto& s : r->stage)
     {
-        s.pos.release(); s.nrm.release(); s.alb.release(); s.idx.release();
+        s.pos.release(); s.nrm.release(); s.alb.release(); s.uv.release(); s.tid.release(); s.idx.release();
     }
     if (r->frames_host)
         cudaFreeHost(r->frames_host);
@@ -676,6 +701,8 @@ edxr_status edxr_set_state(edxr_renderer* r, const edxr_state* s)
         return fail(EDXR_ERR_INVALID_ARG, "unknown depth function");
     if (s->msaa_log2 < 0 || s->msaa_log2 > kMaxMsaaLog2)
         return fail(EDXR_ERR_INVALID_ARG, "msaa_log2 must be in [0, 5] (1 to 32 samples)");
+    if (s->texture_filter < EDXR_FILTER_NEAREST || s->texture_filter > EDXR_FILTER_ANISOTROPIC_16X)
+        return fail(EDXR_ERR_INVALID_ARG, "unknown texture filter");
     r->state = *s;
     return EDXR_OK;
 }
@@ -686,7 +713,7 @@ edxr_status edxr_set_shader(edxr_renderer* r, int vs_kind, int ps_kind, const ed
         return fail(EDXR_ERR_INVALID_ARG, "NULL renderer");
     if (vs_kind != EDXR_VS_DEFAULT)
         return fail(EDXR_ERR_INVALID_ARG, "unknown vertex shader");
-    if (ps_kind < EDXR_PS_BLINN_PHONG || ps_kind > EDXR_PS_LAMBERTIAN)
+    if (ps_kind < EDXR_PS_BLINN_PHONG || ps_kind > EDXR_PS_LAMBERTIAN_TEXTURED)
         return fail(EDXR_ERR_INVALID_ARG, "unknown pixel shader");
     r->shading.ps_kind = ps_kind;
     if (p)
@@ -713,14 +740,91 @@ edxr_status edxr_render(edxr_renderer* r, const edxr_mesh* mesh)
     if ((s = sync_pass(r)) != EDXR_OK)
         return s;
     edxr_mesh dm;
-    if ((s = stage_mesh(r, 0, mesh, &dm)) != EDXR_OK)
+    if ((s = stage_mesh(r, 0, mesh, &dm, r->shading.ps_kind == EDXR_PS_LAMBERTIAN_TEXTURED)) != EDXR_OK)
         return s;
     if ((s = ensure_frames_host(r, 1)) != EDXR_OK)
         return s;
     cudaEventSynchronize(r->done);  // the pinned descriptor may still be in flight
     fill_frame(r->frames_host[0], dm, r->cam, r->shading, r->state.depth_func, r->state.hierarchical, r->width,
-               r->height);
+               r->height, r);
     return launch_frames(r, 1, r->width, r->height, r->state.msaa_log2);
+}
+
+edxr_status edxr_set_textures(edxr_renderer* r, const edxr_texture* textures, uint32_t count)
+{
+    if (!r || (count && !textures))
+        return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
+    uint64_t total = 0;
+    std::vector<TexDesc> desc(count);
+    for (uint32_t i = 0; i < count; i++)
+    {
+        const edxr_texture& t = textures[i];
+        if (t.width == 0 || t.height == 0 || t.width > 16384 || t.height > 16384 || !t.texels ||
+            (t.format != EDXR_TEXTURE_RGBA8 && t.format != EDXR_TEXTURE_RGBA32F))
+            return fail(EDXR_ERR_INVALID_ARG, "texture: size must be in [1, 16384], texels non-NULL, format known");
+        TexDesc& d = desc[i];
+        d.width = t.width;
+        d.height = t.height;
+        d.levels = 1;
+        d.pad = 0;
+        d.base = total;
+        uint32_t w = t.width, h = t.height;
+        total += (uint64_t)w * h;
+        while (w > 1 || h > 1)
+        {
+            w = std::max(1u, w >> 1);
+            h = std::max(1u, h >> 1);
+            total += (uint64_t)w * h;
+            d.levels++;
+        }
+    }
+    DeviceGuard g(r->device);
+    edxr_status s = sync_pass(r);  // frames in flight may still sample the old set
+    if (s != EDXR_OK)
+        return s;
+    EDXR_CUDA(cudaStreamSynchronize(r->stream));
+    r->num_textures = 0;
+    if (count == 0)
+        return EDXR_OK;
+    EDXR_CUDA(r->tex_desc.ensure(sizeof(TexDesc) * count));
+    EDXR_CUDA(r->tex_texels.ensure(sizeof(float4) * total));
+    float4* pool = r->tex_texels.as<float4>();
+    std::vector<float4> level0;
+    for (uint32_t i = 0; i < count; i++)
+    {
+        const edxr_texture& t = textures[i];
+        const TexDesc& d = desc[i];
+        const size_t n = (size_t)t.width * t.height;
+        if (t.format == EDXR_TEXTURE_RGBA8)
+        {
+            // channel = byte / 255 (Color(Color4b), the texel conversion of
+            // an 8-bit image texture)
+            const uint8_t* b = static_cast<const uint8_t*>(t.texels);
+            level0.resize(n);
+            for (size_t k = 0; k < n; k++)
+                level0[k] = make_float4(b[4 * k] / 255.0f, b[4 * k + 1] / 255.0f, b[4 * k + 2] / 255.0f,
+                                        b[4 * k + 3] / 255.0f);
+            EDXR_CUDA(cudaMemcpy(pool + d.base, level0.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+        }
+        else
+            EDXR_CUDA(cudaMemcpy(pool + d.base, t.texels, sizeof(float4) * n, cudaMemcpyHostToDevice));
+        uint64_t off = d.base;
+        uint32_t w = t.width, h = t.height;
+        for (uint32_t l = 1; l < d.levels; l++)
+        {
+            const uint32_t nw = std::max(1u, w >> 1), nh = std::max(1u, h >> 1);
+            EDXR_CUDA(launch_mip_level(pool + off, (int)w, (int)h, pool + off + (uint64_t)w * h, (int)nw, (int)nh,
+                                       r->stream));
+            off += (uint64_t)w * h;
+            w = nw;
+            h = nh;
+        }
+    }
+    EDXR_CUDA(cudaMemcpyAsync(r->tex_desc.ptr, desc.data(), sizeof(TexDesc) * count, cudaMemcpyHostToDevice,
+                              r->stream));
+    EDXR_CUDA(cudaStreamSynchronize(r->stream));
+    r->num_textures = count;
+    return EDXR_OK;
 }
 
 edxr_status edxr_synchronize(edxr_renderer* r)
@@ -895,7 +999,7 @@ edxr_status edxr_render_batched(edxr_renderer* r, const edxr_mesh* meshes, uint3
     {
         if (views[v].mesh >= num_meshes)
             return fail(EDXR_ERR_INVALID_ARG, "view references a mesh out of range");
-        if (views[v].ps_kind < EDXR_PS_BLINN_PHONG || views[v].ps_kind > EDXR_PS_LAMBERTIAN)
+        if (views[v].ps_kind < EDXR_PS_BLINN_PHONG || views[v].ps_kind > EDXR_PS_LAMBERTIAN_TEXTURED)
             return fail(EDXR_ERR_INVALID_ARG, "unknown pixel shader in view");
         if (views[v].depth_func != EDXR_DEPTH_LEQUAL && views[v].depth_func != EDXR_DEPTH_LESS)
             return fail(EDXR_ERR_INVALID_ARG, "unknown depth function in view");
@@ -905,9 +1009,12 @@ edxr_status edxr_render_batched(edxr_renderer* r, const edxr_mesh* meshes, uint3
     DeviceGuard g(r->device);
     if ((s = sync_pass(r)) != EDXR_OK)
         return s;
+    bool textured = false;
+    for (uint32_t v = 0; v < num_views; v++)
+        textured = textured || views[v].ps_kind == EDXR_PS_LAMBERTIAN_TEXTURED;
     std::vector<edxr_mesh> dm(num_meshes);
     for (uint32_t m = 0; m < num_meshes; m++)
-        if ((s = stage_mesh(r, m, &meshes[m], &dm[m])) != EDXR_OK)
+        if ((s = stage_mesh(r, m, &meshes[m], &dm[m], textured)) != EDXR_OK)
             return s;
     if ((s = ensure_frames_host(r, num_views)) != EDXR_OK)
         return s;
@@ -923,7 +1030,7 @@ edxr_status edxr_render_batched(edxr_renderer* r, const edxr_mesh* meshes, uint3
         sh.ps_kind = views[v].ps_kind;
         sh.p = views[v].shading;
         fill_frame(r->frames_host[v], dm[views[v].mesh], cam, sh, views[v].depth_func, r->state.hierarchical, width,
-                   height);
+                   height, r);
     }
     return launch_frames(r, num_views, width, height);
 }
@@ -993,6 +1100,9 @@ edxr_status diff_mesh(edxr_renderer* r, const edxr_mesh* mesh, const edxr_shader
         return fail(EDXR_ERR_INVALID_ARG, "nothing rendered yet");
     if (r->last_samples != 1)
         return fail(EDXR_ERR_UNSUPPORTED, "the differentiable form takes a pass rendered with one sample per pixel");
+    for (uint32_t i = 0; i < r->last_frames; i++)
+        if (r->frames_host[i].ps_kind == EDXR_PS_LAMBERTIAN_TEXTURED)
+            return fail(EDXR_ERR_UNSUPPORTED, "the differentiable form has no adjoint of texture sampling");
     for (uint32_t i = 0; i < r->last_frames; i++)
         if (r->frames_host[i].nv != mesh->num_vertices || r->frames_host[i].nt != mesh->num_triangles)
             return fail(EDXR_ERR_INVALID_ARG, "mesh sizes differ from the mesh of the last pass");

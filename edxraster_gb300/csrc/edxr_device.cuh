@@ -549,9 +549,191 @@ __device__ __forceinline__ float3 shade_model(const FrameDesc& f, float3 P, floa
     {
     case 0: return f3(fmaf(A.x, diffuse, spec), fmaf(A.y, diffuse, spec), fmaf(A.z, diffuse, spec));
     case 1: return f3(diffuse + spec, diffuse + spec, diffuse + spec);
-    case 2: return f3(A.x * diffuse, A.y * diffuse, A.z * diffuse);
+    case 2:
+    case 4: return f3(A.x * diffuse, A.y * diffuse, A.z * diffuse);
     default: return f3(diffuse, diffuse, diffuse);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Texture sampling (Texture2D::Sample(uv, differentials) of the textured
+// Lambertian shader, Shader.h:226-239).  EDXUtil's sampler is not part of the
+// reference; this build's contract, restated operation for operation in the
+// oracle: coordinates repeat; texel (x, y) covers [x, x+1) x [y, y+1) in
+// texel units; nearest and bilinear sample level 0; trilinear takes the
+// level of detail 0.5 log2(max |d|^2) of the two differentials in texels and
+// blends the bilinear samples of the two levels around it; anisotropic Nx
+// takes n = min(N, ceil(major / minor)) trilinear probes along the longer
+// differential, at the level of detail of major / n, and averages them.
+__device__ __forceinline__ float wrap01(float u) { return u - floorf(u); }
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return fmaf(t, b - a, a); }
+__device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t)
+{
+    return make_float4(lerpf(a.x, b.x, t), lerpf(a.y, b.y, t), lerpf(a.z, b.z, t), lerpf(a.w, b.w, t));
+}
+
+struct TexLevel
+{
+    const float4* texels;
+    int w, h;
+};
+
+__device__ __forceinline__ TexLevel tex_level(const FrameDesc& f, const TexDesc& d, int level)
+{
+    uint64_t off = d.base;
+    int w = (int)d.width, h = (int)d.height;
+    for (int l = 0; l < level; l++)
+    {
+        off += (uint64_t)w * h;
+        w = max(1, w >> 1);
+        h = max(1, h >> 1);
+    }
+    return { f.texels + off, w, h };
+}
+
+__device__ __forceinline__ float4 tex_fetch(const TexLevel& L, int x, int y)
+{
+    x %= L.w;
+    if (x < 0) x += L.w;
+    y %= L.h;
+    if (y < 0) y += L.h;
+    return __ldg(L.texels + (size_t)y * L.w + x);
+}
+
+__device__ __forceinline__ float4 tex_bilinear(const TexLevel& L, float u, float v)
+{
+    const float fx = wrap01(u) * (float)L.w - 0.5f, fy = wrap01(v) * (float)L.h - 0.5f;
+    const float x0 = floorf(fx), y0 = floorf(fy);
+    const float tx = fx - x0, ty = fy - y0;
+    const int ix = (int)x0, iy = (int)y0;
+    const float4 a = lerp4(tex_fetch(L, ix, iy), tex_fetch(L, ix + 1, iy), tx);
+    const float4 b = lerp4(tex_fetch(L, ix, iy + 1), tex_fetch(L, ix + 1, iy + 1), tx);
+    return lerp4(a, b, ty);
+}
+
+__device__ __forceinline__ float4 tex_trilinear(const FrameDesc& f, const TexDesc& d, float u, float v, float lod)
+{
+    lod = fminf(fmaxf(lod, 0.0f), (float)(d.levels - 1));
+    const int l0 = (int)floorf(lod);
+    const float t = lod - (float)l0;
+    const float4 c0 = tex_bilinear(tex_level(f, d, l0), u, v);
+    if (t == 0.0f)
+        return c0;
+    return lerp4(c0, tex_bilinear(tex_level(f, d, min(l0 + 1, (int)d.levels - 1)), u, v), t);
+}
+
+__device__ __forceinline__ float4 sample_texture(const FrameDesc& f, const TexDesc& d, float u, float v, float2 d0,
+                                                 float2 d1)
+{
+    switch (f.tex_filter)
+    {
+    case 0:
+    {
+        const TexLevel L = tex_level(f, d, 0);
+        const int x = min((int)floorf(wrap01(u) * (float)L.w), L.w - 1);
+        const int y = min((int)floorf(wrap01(v) * (float)L.h), L.h - 1);
+        return tex_fetch(L, x, y);
+    }
+    case 1: return tex_bilinear(tex_level(f, d, 0), u, v);
+    default: break;
+    }
+    const float ax = d0.x * (float)d.width, ay = d0.y * (float)d.height;
+    const float bx = d1.x * (float)d.width, by = d1.y * (float)d.height;
+    const float r0 = fmaf(ax, ax, ay * ay), r1 = fmaf(bx, bx, by * by);
+    if (f.tex_filter == 2)
+    {
+        const float r = fmaxf(r0, r1);
+        return tex_trilinear(f, d, u, v, r > 1.0f ? 0.5f * log2f(r) : 0.0f);
+    }
+    const int N = f.tex_filter == 3 ? 4 : (f.tex_filter == 4 ? 8 : 16);
+    const float l0 = sqrtf(r0), l1 = sqrtf(r1);
+    const float major = fmaxf(l0, l1), minor = fminf(l0, l1);
+    const int n = major <= 0.0f ? 1 : (minor <= 0.0f ? N : min(N, (int)ceilf(major / minor)));
+    const float2 axis = l0 >= l1 ? d0 : d1;
+    const float m = major / (float)n;
+    const float lod = m > 1.0f ? log2f(m) : 0.0f;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = 0; i < n; i++)
+    {
+        const float s = ((float)i + 0.5f) / (float)n - 0.5f;
+        const float4 c = tex_trilinear(f, d, fmaf(axis.x, s, u), fmaf(axis.y, s, v), lod);
+        acc = make_float4(acc.x + c.x, acc.y + c.y, acc.z + c.z, acc.w + c.w);
+    }
+    const float inv = 1.0f / (float)n;
+    return make_float4(acc.x * inv, acc.y * inv, acc.z * inv, acc.w * inv);
+}
+
+// Perspective-correct barycentrics of triangle t at the centre of pixel
+// (px, py) (TriangleSSE::CalcBarycentricCoord, RasterTriangle.h:333-337, then
+// Fragment::Interpolate, Shader.h:150-158).
+__device__ __forceinline__ float3 persp_bary(const RTri& t, int px, int py)
+{
+    const int cx = (px << 4) + 8, cy = (py << 4) + 8;
+    const Edges e = tri_edges(t);
+    const int n1 = wadd(wmul(e.B[1], wsub(cx, t.v2x)), wmul(e.C[1], wsub(cy, t.v2y)));
+    const int n2 = wadd(wmul(e.B[2], wsub(cx, t.v2x)), wmul(e.C[2], wsub(cy, t.v2y)));
+    float b0 = fmul(__int2float_rn(n1), t.invDet), b1 = fmul(__int2float_rn(n2), t.invDet);
+    float b2 = fsub(fsub(1.0f, b0), b1);
+    b0 = fmul(b0, t.invW0);
+    b1 = fmul(b1, t.invW1);
+    b2 = fmul(b2, t.invW2);
+    const float invB = fdiv(1.0f, fadd(fadd(b0, b1), b2));
+    b0 = fmul(b0, invB);
+    b1 = fmul(b1, invB);
+    return f3(b0, b1, fsub(fsub(1.0f, b0), b1));
+}
+
+// Albedo of the textured Lambertian shader at pixel (px, py) of triangle t:
+// the texture coordinate interpolated there, and the differentials of the
+// pixel's 2x2 quad (LambertianAlbedoPixelShader, Shader.h:226-228: lane 1
+// minus lane 0 and lane 2 minus lane 0, the quad's top-left pixel being
+// lane 0), all from t's perspective-correct barycentrics.
+__device__ __forceinline__ float3 texture_albedo(const FrameDesc& f, const RTri& t, const ClipPoly* polys, int px,
+                                                 int py)
+{
+    const uint32_t tri = t.order >> 4;
+    const uint32_t slot = f.tex_ids ? __ldg(f.tex_ids + tri) : 0u;
+    if (slot >= f.num_textures || !f.uvs)
+        return f3(1.0f, 1.0f, 1.0f);
+    float2 uv[3];
+    {
+        const uint32_t i0 = __ldg(f.indices + 3 * (size_t)tri + 0);
+        const uint32_t i1 = __ldg(f.indices + 3 * (size_t)tri + 1);
+        const uint32_t i2 = __ldg(f.indices + 3 * (size_t)tri + 2);
+        const float* p0 = reinterpret_cast<const float*>(f.uvs + (size_t)i0 * f.uv_stride);
+        const float* p1 = reinterpret_cast<const float*>(f.uvs + (size_t)i1 * f.uv_stride);
+        const float* p2 = reinterpret_cast<const float*>(f.uvs + (size_t)i2 * f.uv_stride);
+        const float2 s[3] = { make_float2(__ldg(p0), __ldg(p0 + 1)), make_float2(__ldg(p1), __ldg(p1 + 1)),
+                              make_float2(__ldg(p2), __ldg(p2 + 1)) };
+        if (t.poly == kUnclipped)
+        {
+            uv[0] = s[0]; uv[1] = s[1]; uv[2] = s[2];
+        }
+        else
+        {
+            const ClipPoly& P = polys[t.poly >> 4];
+            const int fk = (int)(t.poly & 15u);
+            const int pv[3] = { 0, fk - 1, fk };
+#pragma unroll
+            for (int k = 0; k < 3; k++)
+            {
+                const float w0 = P.w[pv[k]][0], w1 = P.w[pv[k]][1], w2 = P.w[pv[k]][2];
+                uv[k] = make_float2(fadd(fadd(fmul(w0, s[0].x), fmul(w1, s[1].x)), fmul(w2, s[2].x)),
+                                    fadd(fadd(fmul(w0, s[0].y), fmul(w1, s[1].y)), fmul(w2, s[2].y)));
+            }
+        }
+    }
+    auto uv_at = [&](int x, int y) {
+        const float3 b = persp_bary(t, x, y);
+        return make_float2(fmaf(b.x, uv[0].x, fmaf(b.y, uv[1].x, b.z * uv[2].x)),
+                           fmaf(b.x, uv[0].y, fmaf(b.y, uv[1].y, b.z * uv[2].y)));
+    };
+    const int qx = px & ~1, qy = py & ~1;
+    const float2 q0 = uv_at(qx, qy), q1 = uv_at(qx + 1, qy), q2 = uv_at(qx, qy + 1);
+    const float2 here = (px == qx && py == qy) ? q0 : (py == qy ? q1 : (px == qx ? q2 : uv_at(px, py)));
+    const float4 c = sample_texture(f, f.textures[slot], here.x, here.y, make_float2(q1.x - q0.x, q1.y - q0.y),
+                                    make_float2(q2.x - q0.x, q2.y - q0.y));
+    return f3(c.x, c.y, c.z);
 }
 
 // BlinnPhongPixelShader as written (ks = 3, exponent 200, no clamp) amplifies
@@ -600,7 +782,7 @@ static __device__ __noinline__ float3 shade_fragment_fp64(const FrameDesc& f, co
 // Fragment::Interpolate (Shader.h:142-170) from the fragment's barycentrics,
 // then the shading model.
 __device__ __forceinline__ float3 shade_fragment(const FrameDesc& f, const RTri& t, const ClipPoly* polys,
-                                                 float l0, float l1)
+                                                 float l0, float l1, int px, int py)
 {
     if (f.ps_kind == 1)
         return shade_fragment_fp64(f, t, polys, l0, l1);
@@ -616,7 +798,7 @@ __device__ __forceinline__ float3 shade_fragment(const FrameDesc& f, const RTri&
     const ShadeVerts v = shade_verts(f, t, polys);
     const float3 P = lerp3(b0, v.p[0], b1, v.p[1], b2, v.p[2]);
     const float3 N = lerp3(b0, v.n[0], b1, v.n[1], b2, v.n[2]);
-    const float3 A = lerp3(b0, v.a[0], b1, v.a[1], b2, v.a[2]);
+    const float3 A = f.ps_kind == 4 ? texture_albedo(f, t, polys, px, py) : lerp3(b0, v.a[0], b1, v.a[1], b2, v.a[2]);
     return shade_model(f, P, N, A);
 }
 

@@ -40,6 +40,15 @@ constexpr uint64_t item_capacity(uint64_t tiles, uint64_t bin_capacity) { return
 // collinear vertices can add a few more, so the working polygon has room.
 constexpr int kMaxPolygon = 16;
 
+// One texture slot in device memory: level l (of `levels`, each half the
+// size of the one before, down to 1x1) starts at texel base + sum of the
+// sizes of the levels before it.
+struct TexDesc
+{
+    uint32_t width, height, levels, pad;
+    uint64_t base;
+};
+
 // Per frame (one view of one mesh).  Kernels read it from global memory.
 struct FrameDesc
 {
@@ -68,6 +77,12 @@ struct FrameDesc
     float pad2;
     double eye_d[3];           // eye position in double (FP64 shading)
     double ndc_from_raster_d[6];  // the raster-to-NDC inverse in double (differentiable form)
+    // textures of the textured Lambertian shader
+    const uint32_t* tex_ids;      // per input triangle (NULL: slot 0)
+    const TexDesc* textures;
+    const float4* texels;
+    uint32_t num_textures;
+    int tex_filter;               // edxr_texture_filter
 };
 
 // One triangle after clipping and setup (RasterTriangle, RasterTriangle.h:11-24),
@@ -166,6 +181,9 @@ Tuning default_tuning();
 void record_error(const char* msg);
 void prepare_kernels();
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s);
+// One mip level: each texel the mean of the 2x2 texels above it (indices
+// clamped to the source size).
+cudaError_t launch_mip_level(const float4* src, int sw, int sh, float4* dst, int dw, int dh, cudaStream_t s);
 // Mesh used by the differentiable form (device pointers, strides in bytes).
 struct DiffMesh
 {

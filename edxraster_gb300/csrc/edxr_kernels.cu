@@ -939,7 +939,7 @@ static __device__ __noinline__ void write_pixel(const PixelOut a, const FrameDes
     const float L1 = fmul(__int2float_rn(n2), t.invDet);
     const float L2 = fsub(fsub(1.0f, L0), L1);
     const float d = fadd(fadd(fmul(L0, t.z0), fmul(L1, t.z1)), fmul(L2, t.z2));
-    const float3 c = shade_fragment(f, t, a.polys, L0, L1);
+    const float3 c = shade_fragment(f, t, a.polys, L0, L1, px, py);
     a.color[pix] = make_float4(c.x, c.y, c.z, 1.0f);
     a.depth[pix] = d;
     a.tri_id[pix] = t.order >> 4;
@@ -1251,7 +1251,7 @@ static __device__ __noinline__ void write_pixel_ms(const PassArgs& a, const Fram
         if (r != last)
         {
             depth_at(t, (px << 4) + 8, (py << 4) + 8, L0, L1);
-            const float3 c = shade_fragment(f, t, a.polys, L0, L1);
+            const float3 c = shade_fragment(f, t, a.polys, L0, L1, px, py);
             c8[0] = to_byte(c.x);
             c8[1] = to_byte(c.y);
             c8[2] = to_byte(c.z);
@@ -1561,6 +1561,28 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
 int kernels_per_pass(const PassArgs& a)
 {
     return 5 + (a.total_tris ? 2 : 0);
+}
+
+__global__ void k_mip_level(const float4* src, int sw, int sh, float4* dst, int dw, int dh)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= dw * dh)
+        return;
+    const int x = i % dw, y = i / dw;
+    const int x0 = min(2 * x, sw - 1), x1 = min(2 * x + 1, sw - 1);
+    const int y0 = min(2 * y, sh - 1), y1 = min(2 * y + 1, sh - 1);
+    const float4 a = src[(size_t)y0 * sw + x0], b = src[(size_t)y0 * sw + x1];
+    const float4 c = src[(size_t)y1 * sw + x0], d = src[(size_t)y1 * sw + x1];
+    auto avg = [](float p, float q, float r, float t) { return fmul(fadd(fadd(fadd(p, q), r), t), 0.25f); };
+    dst[i] = make_float4(avg(a.x, b.x, c.x, d.x), avg(a.y, b.y, c.y, d.y), avg(a.z, b.z, c.z, d.z),
+                         avg(a.w, b.w, c.w, d.w));
+}
+
+cudaError_t launch_mip_level(const float4* src, int sw, int sh, float4* dst, int dw, int dh, cudaStream_t s)
+{
+    const int n = dw * dh;
+    k_mip_level<<<(n + 255) / 256, 256, 0, s>>>(src, sw, sh, dst, dw, dh);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s)

@@ -185,6 +185,8 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
         return noalloc_fail(EDXR_ERR_INVALID_ARG, "unknown depth function");
     if (state->msaa_log2 != 0)
         return noalloc_fail(EDXR_ERR_UNSUPPORTED, "edxr_render_noalloc renders one sample per pixel (msaa_log2 must be 0)");
+    if (ps_kind == EDXR_PS_LAMBERTIAN_TEXTURED)
+        return noalloc_fail(EDXR_ERR_UNSUPPORTED, "edxr_render_noalloc holds no texture slots");
     if (ps_kind < EDXR_PS_BLINN_PHONG || ps_kind > EDXR_PS_LAMBERTIAN)
         return noalloc_fail(EDXR_ERR_INVALID_ARG, "unknown pixel shader");
     const double ln = sqrt((double)params->light[0] * params->light[0] + (double)params->light[1] * params->light[1] +

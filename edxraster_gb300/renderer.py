@@ -20,6 +20,10 @@ from ._lib import EdxrError  # noqa: F401  (re-exported)
 
 DEPTH_LEQUAL, DEPTH_LESS = 0, 1
 PS_BLINN_PHONG, PS_BLINN_PHONG_REFERENCE, PS_LAMBERTIAN_ALBEDO, PS_LAMBERTIAN = 0, 1, 2, 3
+PS_LAMBERTIAN_TEXTURED = 4
+# TextureFilter (RenderStates.h:23)
+FILTER_NEAREST, FILTER_LINEAR, FILTER_TRILINEAR = 0, 1, 2
+FILTER_ANISOTROPIC_4X, FILTER_ANISOTROPIC_8X, FILTER_ANISOTROPIC_16X = 3, 4, 5
 
 
 def _f16(m):
@@ -30,7 +34,7 @@ def _f16(m):
 class DeviceMesh:
     """A mesh resident in device memory (torch CUDA tensors), passed by pointer."""
 
-    def __init__(self, positions, indices, normals=None, albedo=None, uvs=None):
+    def __init__(self, positions, indices, normals=None, albedo=None, uvs=None, texture_ids=None):
         import torch
         dev = positions.device
 
@@ -48,12 +52,19 @@ class DeviceMesh:
         self.normals = prep(normals, torch.float32, 3)
         self.albedo = prep(albedo, torch.float32, 3)
         self.uvs = prep(uvs, torch.float32, 2)
+        self.texture_ids = None
+        if texture_ids is not None:
+            ids = texture_ids if isinstance(texture_ids, torch.Tensor) else torch.from_numpy(
+                np.ascontiguousarray(texture_ids).astype(np.int32))
+            self.texture_ids = ids.to(device=dev, dtype=torch.int32).contiguous().view(-1)
 
     @classmethod
     def from_mesh(cls, mesh, device="cuda"):
         import torch
         t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)  # noqa: E731
-        return cls(t(mesh.positions), t(mesh.indices.astype(np.int32)), t(mesh.normals), t(mesh.albedo), t(mesh.uvs))
+        tid = getattr(mesh, "texture_ids", None)
+        return cls(t(mesh.positions), t(mesh.indices.astype(np.int32)), t(mesh.normals), t(mesh.albedo), t(mesh.uvs),
+                   None if tid is None else t(tid.astype(np.int32)))
 
     @property
     def nv(self):
@@ -66,7 +77,7 @@ class DeviceMesh:
     def abi(self) -> _lib.Mesh:
         p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
         return _lib.Mesh(p(self.positions), 12, p(self.normals), 12, p(self.uvs), 8, p(self.albedo), 12,
-                         p(self.indices), self.nv, self.nt, _lib.MEMORY_DEVICE)
+                         p(self.indices), self.nv, self.nt, _lib.MEMORY_DEVICE, p(self.texture_ids))
 
 
 class HostMesh:
@@ -89,6 +100,8 @@ class HostMesh:
         self.albedo = prep(mesh.albedo, np.float32)
         self.uvs = prep(mesh.uvs, np.float32)
         self.indices = prep(mesh.indices, np.uint32)
+        tid = getattr(mesh, "texture_ids", None)
+        self.texture_ids = None if tid is None else prep(tid, np.uint32)
         self.nv, self.nt = int(self.positions.shape[0]), int(self.indices.shape[0])
 
     def nbytes(self) -> int:
@@ -97,8 +110,10 @@ class HostMesh:
         return sum(a.nbytes for a in (self.positions, self.normals, self.albedo, self.indices))
 
     def abi(self) -> _lib.Mesh:
+        tid = None if self.texture_ids is None else self.texture_ids.ctypes.data
         return _lib.Mesh(self.positions.ctypes.data, 12, self.normals.ctypes.data, 12, self.uvs.ctypes.data, 8,
-                         self.albedo.ctypes.data, 12, self.indices.ctypes.data, self.nv, self.nt, _lib.MEMORY_HOST)
+                         self.albedo.ctypes.data, 12, self.indices.ctypes.data, self.nv, self.nt, _lib.MEMORY_HOST,
+                         tid)
 
 
 def _as_abi_mesh(mesh):
@@ -182,9 +197,27 @@ class Renderer:
         return 1 << self._state.msaa_log2
 
     def SetTextureFilter(self, texture_filter: int):
-        """Renderer::SetTextureFilter (Renderer.h:48); stored, no texture sampling here."""
+        """Renderer::SetTextureFilter (Renderer.h:48): FILTER_* (trilinear is the reference default)."""
+        old = self._state.texture_filter
         self._state.texture_filter = int(texture_filter)
-        _lib.check(self._lib.edxr_set_state(self._h, ctypes.byref(self._state)))
+        try:
+            _lib.check(self._lib.edxr_set_state(self._h, ctypes.byref(self._state)))
+        except Exception:
+            self._state.texture_filter = old
+            raise
+
+    def SetTextures(self, textures):
+        """The texture slots (Mesh::GetTextures / RenderStates::TextureSlots): a list of
+        (H, W, 4) arrays, uint8 (RGBA8) or float32 (RGBA32F); row 0 at v = 0."""
+        arrs, descs = [], []
+        for t in textures:
+            a = np.ascontiguousarray(t)
+            if a.ndim != 3 or a.shape[2] != 4 or a.dtype not in (np.uint8, np.float32):
+                raise ValueError("a texture is an (H, W, 4) uint8 or float32 array")
+            arrs.append(a)
+            descs.append(_lib.Texture(a.shape[1], a.shape[0], 0 if a.dtype == np.uint8 else 1, a.ctypes.data))
+        arr = (_lib.Texture * max(1, len(descs)))(*descs)
+        _lib.check(self._lib.edxr_set_textures(self._h, arr, len(descs)))
 
     def SetHierarchicalRasterize(self, h: bool):
         """Renderer::SetHierarchicalRasterize (Renderer.h:49)."""

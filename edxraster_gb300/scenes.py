@@ -23,6 +23,7 @@ SHADER_BLINN_PHONG = 0
 SHADER_BLINN_PHONG_REFERENCE = 1
 SHADER_LAMBERTIAN_ALBEDO = 2
 SHADER_LAMBERTIAN = 3
+SHADER_LAMBERTIAN_TEXTURED = 4
 
 DEPTH_LEQUAL = 0
 DEPTH_LESS = 1
@@ -50,6 +51,7 @@ class Mesh:
     albedo: np.ndarray     # (nv,3) float32
     uvs: np.ndarray        # (nv,2) float32
     indices: np.ndarray    # (nt,3) uint32
+    texture_ids: np.ndarray = None  # (nt,) uint32 texture slot per triangle, None = slot 0
 
     @property
     def nv(self) -> int:
@@ -197,6 +199,53 @@ def torus(nu: int, nv: int, R: float = 1.0, r: float = 0.35, center=(0, 0, 0)) -
     idx = _orient_outward(pos, idx, out).astype(np.uint32)
     return Mesh(pos.astype(np.float32), nrm.astype(np.float32),
                 np.ones((len(pos), 3), np.float32), uv.astype(np.float32), idx)
+
+
+def test_textures(seed: int = 0):
+    """Three texture slots: an 8-bit 64x64 checkerboard with noise, a float
+    48x20 gradient (non-square, odd mip chain) and a 1x1 constant colour (the
+    reference's ConstantTexture2D)."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:64, 0:64]
+    check = (((x // 8) + (y // 8)) % 2).astype(np.float64)
+    rgba8 = np.stack([200 * check + 40, 120 + 80 * (1 - check), rng.integers(0, 256, (64, 64)),
+                      np.full((64, 64), 255)], -1).astype(np.uint8)
+    gy, gx = np.mgrid[0:20, 0:48]
+    grad = np.stack([gx / 47.0, gy / 19.0, 0.5 + 0.5 * np.sin(gx * 0.7), np.ones_like(gx, dtype=np.float64)],
+                    -1).astype(np.float32)
+    const = np.array([[[0.9, 0.6, 0.3, 1.0]]], np.float32)
+    return [rgba8, grad, const]
+
+
+def textured_scene(width=320, height=180, seed=0) -> Scene:
+    """A textured sphere and a ground plane seen at a grazing angle (strongly
+    anisotropic texture footprints), texture coordinates repeating several
+    times; triangles cycle through the slots of test_textures()."""
+    sph = uv_sphere(24, 16, 1.0, center=(0.0, 0.2, 0.0))
+    sph.uvs = (sph.uvs * np.array([4.0, 2.0], np.float32)).astype(np.float32)
+    n = 24
+    gx, gz = np.meshgrid(np.linspace(-6.0, 6.0, n + 1), np.linspace(-2.0, 14.0, n + 1), indexing="xy")
+    gpos = np.stack([gx, np.full_like(gx, -1.0), gz], -1).reshape(-1, 3)
+    guv = np.stack([gx * 0.75, gz * 0.75], -1).reshape(-1, 2)
+    a = (np.arange(n)[None, :] + (n + 1) * np.arange(n)[:, None]).ravel()
+    quads = np.stack([a, a + n + 1, a + 1, a + 1, a + n + 1, a + n + 2], -1).reshape(-1, 3)
+    g = Mesh(gpos.astype(np.float32), np.tile([[0.0, 1.0, 0.0]], (len(gpos), 1)).astype(np.float32),
+             np.ones((len(gpos), 3), np.float32), guv.astype(np.float32), quads.astype(np.uint32))
+    cent = g.positions[g.indices].mean(axis=1)
+    g.indices = _orient_outward(g.positions, g.indices.astype(np.int64), np.tile([0.0, 1.0, 0.0], (len(cent), 1))
+                                ).astype(np.uint32)
+    off = sph.nv
+    mesh = Mesh(np.concatenate([sph.positions, g.positions]), np.concatenate([sph.normals, g.normals]),
+                np.ones((sph.nv + g.nv, 3), np.float32), np.concatenate([sph.uvs, g.uvs]),
+                np.concatenate([sph.indices, g.indices + off]).astype(np.uint32))
+    mesh.texture_ids = (np.arange(mesh.nt) % 3).astype(np.uint32)
+    mesh.texture_ids[sph.nt:] = 0
+    view = View(width, height,
+                look_at_lh((0.0, 0.6, -3.2), (0.0, -0.2, 2.0), (0, 1, 0)),
+                perspective_lh(60.0, width / height, 0.1, 100.0),
+                raster_matrix(width, height),
+                np.array([0.3, 1.0, -0.4], np.float32), 0.0, 1.0, SHADER_LAMBERTIAN_TEXTURED, DEPTH_LEQUAL)
+    return Scene("textured", mesh, view)
 
 
 # --------------------------------------------------------------------------

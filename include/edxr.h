@@ -85,8 +85,41 @@ typedef enum edxr_ps_kind
      * place of the texture lookup                                             */
     EDXR_PS_LAMBERTIAN_ALBEDO = 2,
     /* LambertianPixelShader (Shader.h:185-207)                                */
-    EDXR_PS_LAMBERTIAN = 3
+    EDXR_PS_LAMBERTIAN = 3,
+    /* LambertianAlbedoPixelShader as written (Shader.h:209-244): the albedo is
+     * sampled from the triangle's texture (edxr_set_textures, the mesh's
+     * per-triangle texture ids) with the state's texture filter; the mesh
+     * needs texture coordinates                                              */
+    EDXR_PS_LAMBERTIAN_TEXTURED = 4
 } edxr_ps_kind;
+
+/* Texture filters (TextureFilter of RenderStates::TexFilter, RenderStates.h:23;
+ * the reference's default is trilinear, RenderStates.h:60). */
+typedef enum edxr_texture_filter
+{
+    EDXR_FILTER_NEAREST = 0,
+    EDXR_FILTER_LINEAR = 1,
+    EDXR_FILTER_TRILINEAR = 2,
+    EDXR_FILTER_ANISOTROPIC_4X = 3,
+    EDXR_FILTER_ANISOTROPIC_8X = 4,
+    EDXR_FILTER_ANISOTROPIC_16X = 5
+} edxr_texture_filter;
+
+typedef enum edxr_texture_format
+{
+    EDXR_TEXTURE_RGBA8 = 0,    /* 4 bytes per texel, channel = byte / 255      */
+    EDXR_TEXTURE_RGBA32F = 1   /* 16 bytes per texel                           */
+} edxr_texture_format;
+
+/* One texture (Texture2D<Color> of Mesh::mTextures, Mesh.h:25): texels in rows
+ * of `width`, row 0 at v = 0; coordinates repeat.  A 1x1 texture is the
+ * reference's ConstantTexture2D. */
+typedef struct edxr_texture
+{
+    uint32_t width, height;
+    int format;                /* edxr_texture_format                          */
+    const void* texels;        /* host memory, copied by edxr_set_textures     */
+} edxr_texture;
 
 typedef struct edxr_init
 {
@@ -100,7 +133,7 @@ typedef struct edxr_state
     int depth_func;          /* edxr_depth_func                              */
     int hierarchical;        /* RenderStates::HierarchicalRasterize (1)      */
     int msaa_log2;           /* RenderStates::MultiSampleLevel: 0..5 = 1..32 samples */
-    int texture_filter;      /* RenderStates::TexFilter; stored only         */
+    int texture_filter;      /* RenderStates::TexFilter: edxr_texture_filter  */
 } edxr_state;
 
 typedef struct edxr_shader_params
@@ -125,6 +158,9 @@ typedef struct edxr_mesh
     uint32_t num_vertices;
     uint32_t num_triangles;
     int memory;                                      /* edxr_memory    */
+    /* per-triangle texture slot (Mesh::mTexIdx, Mesh.h:26; Clipper.h:95), in
+     * the same memory as the other arrays; NULL: slot 0 for every triangle */
+    const uint32_t* texture_ids;
 } edxr_mesh;
 
 /* Renderer-owned device buffers, valid until the next render or resize.
@@ -177,6 +213,12 @@ edxr_status edxr_set_state(edxr_renderer* r, const edxr_state* state);
  * Renderer.cpp:40-41).  params may be NULL for the defaults. */
 edxr_status edxr_set_shader(edxr_renderer* r, int vs_kind, int ps_kind,
                             const edxr_shader_params* params);
+
+/* The texture slots (RenderStates::TextureSlots, RenderStates.h:28, filled
+ * from Mesh::GetTextures in RenderMesh, Renderer.cpp:106): copies the texels
+ * and builds each texture's mip chain on the device (box filter).  Replaces
+ * the previous set; count 0 clears it. */
+edxr_status edxr_set_textures(edxr_renderer* r, const edxr_texture* textures, uint32_t count);
 
 /* Renderer::RenderMesh, Renderer.cpp:100-118: clear, then render one mesh. */
 edxr_status edxr_render(edxr_renderer* r, const edxr_mesh* mesh);

@@ -275,6 +275,7 @@ typedef struct
     float* l0; float* l1;
     long long* tileFrags;
     double eye[3];
+    struct otex* tex; /* texture slots with their mip chains */
 } frame;
 
 static int push_rv(frame* f, const rvert* v)
@@ -888,6 +889,7 @@ void edxr_oracle_shade(const edxr_oracle_params* P, const double b[3],
         for (int q = 0; q < 3; q++) rgb[q] = diffuse + spec;
         break;
     case EDXR_ORACLE_PS_LAMBERTIAN_ALBEDO:
+    case EDXR_ORACLE_PS_LAMBERTIAN_TEXTURED:
         for (int q = 0; q < 3; q++) rgb[q] = A[q] * diffuse;
         break;
     default:
@@ -896,9 +898,228 @@ void edxr_oracle_shade(const edxr_oracle_params* P, const double b[3],
     }
 }
 
+/* ------------------------------------------------------------------------ */
+/* Texture sampling of the textured Lambertian shader (Shader.h:226-239).
+ * EDXUtil's sampler is absent; this is the build's contract, restated in
+ * FP32 with the kernels' operations: coordinates repeat; nearest and bilinear
+ * sample level 0; trilinear blends the bilinear samples of the two levels
+ * around lod = 0.5 log2(max |d|^2) (differentials in texels); anisotropic Nx
+ * averages n = min(N, ceil(major / minor)) trilinear probes along the longer
+ * differential at the lod of major / n.  Mip level l+1 texel = mean of the
+ * 2x2 texels of level l (indices clamped), summed in order then times 0.25. */
+typedef struct otex
+{
+    int w, h, levels;
+    float* texels; /* RGBA, all levels one after the other */
+} otex;
+
+typedef struct
+{
+    const float* t;
+    int w, h;
+} olevel;
+
+static olevel tex_level(const otex* x, int level)
+{
+    size_t off = 0;
+    int w = x->w, h = x->h;
+    for (int l = 0; l < level; l++)
+    {
+        off += (size_t)w * h;
+        w = w > 1 ? w >> 1 : 1;
+        h = h > 1 ? h >> 1 : 1;
+    }
+    olevel L = { x->texels + 4 * off, w, h };
+    return L;
+}
+
+static int build_texture(const edxr_oracle_texture* in, otex* out)
+{
+    size_t total = 0;
+    int w = in->width, h = in->height, levels = 1;
+    total += (size_t)w * h;
+    while (w > 1 || h > 1)
+    {
+        w = w > 1 ? w >> 1 : 1;
+        h = h > 1 ? h >> 1 : 1;
+        total += (size_t)w * h;
+        levels++;
+    }
+    out->w = in->width;
+    out->h = in->height;
+    out->levels = levels;
+    out->texels = (float*)malloc(total * 4 * sizeof(float));
+    if (!out->texels) return -1;
+    const size_t n0 = (size_t)in->width * in->height;
+    for (size_t k = 0; k < 4 * n0; k++)
+        out->texels[k] = in->format == 0 ? ((const unsigned char*)in->texels)[k] / 255.0f
+                                         : ((const float*)in->texels)[k];
+    for (int l = 1; l < levels; l++)
+    {
+        const olevel a = tex_level(out, l - 1), b = tex_level(out, l);
+        float* dst = (float*)b.t;
+        for (int y = 0; y < b.h; y++)
+            for (int x = 0; x < b.w; x++)
+            {
+                const int x0 = imin(2 * x, a.w - 1), x1 = imin(2 * x + 1, a.w - 1);
+                const int y0 = imin(2 * y, a.h - 1), y1 = imin(2 * y + 1, a.h - 1);
+                for (int c = 0; c < 4; c++)
+                {
+                    const float s = ((a.t[4 * ((size_t)y0 * a.w + x0) + c] + a.t[4 * ((size_t)y0 * a.w + x1) + c]) +
+                                     a.t[4 * ((size_t)y1 * a.w + x0) + c]) + a.t[4 * ((size_t)y1 * a.w + x1) + c];
+                    dst[4 * ((size_t)y * b.w + x) + c] = s * 0.25f;
+                }
+            }
+    }
+    return 0;
+}
+
+static float wrap01(float u) { return u - floorf(u); }
+static float lerpf(float a, float b, float t) { return fmaf(t, b - a, a); }
+
+static void tex_fetch(const olevel* L, int x, int y, float c[4])
+{
+    x %= L->w;
+    if (x < 0) x += L->w;
+    y %= L->h;
+    if (y < 0) y += L->h;
+    const float* p = L->t + 4 * ((size_t)y * L->w + x);
+    for (int k = 0; k < 4; k++) c[k] = p[k];
+}
+
+static void tex_bilinear(const olevel* L, float u, float v, float c[4])
+{
+    const float fx = wrap01(u) * (float)L->w - 0.5f, fy = wrap01(v) * (float)L->h - 0.5f;
+    const float x0 = floorf(fx), y0 = floorf(fy);
+    const float tx = fx - x0, ty = fy - y0;
+    const int ix = (int)x0, iy = (int)y0;
+    float a[4], b[4], p[4], q[4];
+    tex_fetch(L, ix, iy, a);
+    tex_fetch(L, ix + 1, iy, b);
+    tex_fetch(L, ix, iy + 1, p);
+    tex_fetch(L, ix + 1, iy + 1, q);
+    for (int k = 0; k < 4; k++)
+        c[k] = lerpf(lerpf(a[k], b[k], tx), lerpf(p[k], q[k], tx), ty);
+}
+
+static void tex_trilinear(const otex* x, float u, float v, float lod, float c[4])
+{
+    lod = fminf(fmaxf(lod, 0.0f), (float)(x->levels - 1));
+    const int l0 = (int)floorf(lod);
+    const float t = lod - (float)l0;
+    olevel L0 = tex_level(x, l0);
+    tex_bilinear(&L0, u, v, c);
+    if (t == 0.0f)
+        return;
+    olevel L1 = tex_level(x, imin(l0 + 1, x->levels - 1));
+    float d[4];
+    tex_bilinear(&L1, u, v, d);
+    for (int k = 0; k < 4; k++) c[k] = lerpf(c[k], d[k], t);
+}
+
+static void sample_texture(const otex* x, int filter, float u, float v, const float d0[2], const float d1[2],
+                           float c[4])
+{
+    if (filter == 0)
+    {
+        olevel L = tex_level(x, 0);
+        const int ix = imin((int)floorf(wrap01(u) * (float)L.w), L.w - 1);
+        const int iy = imin((int)floorf(wrap01(v) * (float)L.h), L.h - 1);
+        tex_fetch(&L, ix, iy, c);
+        return;
+    }
+    if (filter == 1)
+    {
+        olevel L = tex_level(x, 0);
+        tex_bilinear(&L, u, v, c);
+        return;
+    }
+    const float ax = d0[0] * (float)x->w, ay = d0[1] * (float)x->h;
+    const float bx = d1[0] * (float)x->w, by = d1[1] * (float)x->h;
+    const float r0 = fmaf(ax, ax, ay * ay), r1 = fmaf(bx, bx, by * by);
+    if (filter == 2)
+    {
+        const float r = fmaxf(r0, r1);
+        tex_trilinear(x, u, v, r > 1.0f ? 0.5f * log2f(r) : 0.0f, c);
+        return;
+    }
+    const int N = filter == 3 ? 4 : (filter == 4 ? 8 : 16);
+    const float l0 = sqrtf(r0), l1 = sqrtf(r1);
+    const float major = fmaxf(l0, l1), minor = fminf(l0, l1);
+    const int n = major <= 0.0f ? 1 : (minor <= 0.0f ? N : imin(N, (int)ceilf(major / minor)));
+    const float* axis = l0 >= l1 ? d0 : d1;
+    const float m = major / (float)n;
+    const float lod = m > 1.0f ? log2f(m) : 0.0f;
+    float acc[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+    for (int i = 0; i < n; i++)
+    {
+        const float sft = ((float)i + 0.5f) / (float)n - 0.5f;
+        float p[4];
+        tex_trilinear(x, fmaf(axis[0], sft, u), fmaf(axis[1], sft, v), lod, p);
+        for (int k = 0; k < 4; k++) acc[k] = acc[k] + p[k];
+    }
+    const float inv = 1.0f / (float)n;
+    for (int k = 0; k < 4; k++) c[k] = acc[k] * inv;
+}
+
+/* Perspective-correct barycentrics of raster triangle t at the centre of
+ * pixel (px, py), in float as the kernels form them (RasterTriangle.h:333-337,
+ * Shader.h:150-158). */
+static void persp_bary(const frame* f, const rtri* t, int px, int py, float b[3])
+{
+    const int cx = (px << 4) + 8, cy = (py << 4) + 8;
+    const int e1 = wadd(wmul(t->B1, wsub(cx, t->v2x)), wmul(t->C1, wsub(cy, t->v2y)));
+    const int e2 = wadd(wmul(t->B2, wsub(cx, t->v2x)), wmul(t->C2, wsub(cy, t->v2y)));
+    float b0 = (float)e1 * t->invDet, b1 = (float)e2 * t->invDet;
+    float b2 = (1.0f - b0) - b1;
+    b0 = b0 * f->rv[t->vid[0]].invW;
+    b1 = b1 * f->rv[t->vid[1]].invW;
+    b2 = b2 * f->rv[t->vid[2]].invW;
+    const float invB = 1.0f / ((b0 + b1) + b2);
+    b0 = b0 * invB;
+    b1 = b1 * invB;
+    b[0] = b0;
+    b[1] = b1;
+    b[2] = (1.0f - b0) - b1;
+}
+
+/* Albedo of the textured shader at pixel (px, py): the texture coordinate
+ * there and the differentials of the pixel's 2x2 quad (lane 1 - lane 0,
+ * lane 2 - lane 0; Shader.h:226-228). */
+static void texture_albedo(const frame* f, int ti, int px, int py, double alb[3])
+{
+    const rtri* t = &f->rt[ti];
+    const edxr_oracle_mesh* M = f->M;
+    const uint32_t slot = M->texture_ids ? M->texture_ids[t->texId] : 0u;
+    if (slot >= (uint32_t)f->P->num_textures || !M->uvs)
+    {
+        alb[0] = alb[1] = alb[2] = 1.0;
+        return;
+    }
+    const float* uv[3] = { f->rv[t->vid[0]].uv, f->rv[t->vid[1]].uv, f->rv[t->vid[2]].uv };
+    float q[4][2];
+    const int qx = px & ~1, qy = py & ~1;
+    const int lx[4] = { qx, qx + 1, qx, px }, ly[4] = { qy, qy, qy + 1, py };
+    for (int k = 0; k < 4; k++)
+    {
+        float b[3];
+        persp_bary(f, t, lx[k], ly[k], b);
+        for (int c = 0; c < 2; c++)
+            q[k][c] = fmaf(b[0], uv[0][c], fmaf(b[1], uv[1][c], b[2] * uv[2][c]));
+    }
+    const float d0[2] = { q[1][0] - q[0][0], q[1][1] - q[0][1] };
+    const float d1[2] = { q[2][0] - q[0][0], q[2][1] - q[0][1] };
+    float c[4];
+    sample_texture(&f->tex[slot], f->P->texture_filter, q[3][0], q[3][1], d0, d1, c);
+    alb[0] = c[0];
+    alb[1] = c[1];
+    alb[2] = c[2];
+}
+
 /* Fragment::Interpolate (Shader.h:142-170) in FP64 from the winner's float
- * barycentrics, then the shading model. */
-static void shade_pixel(const frame* f, int ti, float l0, float l1, double rgb[3])
+ * barycentrics, then the shading model; the textured shader's albedo is the
+ * texture sample at pixel (px, py). */
+static void shade_pixel(const frame* f, int ti, float l0, float l1, int px, int py, double rgb[3])
 {
     const rtri* t = &f->rt[ti];
     const edxr_oracle_mesh* M = f->M;
@@ -929,6 +1150,14 @@ static void shade_pixel(const frame* f, int ti, float l0, float l1, double rgb[3
     b[0] *= s;
     b[1] *= s;
     b[2] = 1.0 - b[0] - b[1];
+    if (f->P->shader == EDXR_ORACLE_PS_LAMBERTIAN_TEXTURED)
+    {
+        double a[3];
+        texture_albedo(f, ti, px, py, a);
+        for (int k = 0; k < 3; k++)
+            for (int q = 0; q < 3; q++)
+                alb[k][q] = a[q];
+    }
     edxr_oracle_shade(f->P, b, pos, nrm, alb, f->eye, rgb);
 }
 
@@ -1007,7 +1236,7 @@ static void shade_pixel_ms(frame* f, edxr_oracle_out* out, int x, int y)
         const int e1 = wadd(wmul(t->B1, wsub(cx, t->v2x)), wmul(t->C1, wsub(cy, t->v2y)));
         const int e2 = wadd(wmul(t->B2, wsub(cx, t->v2x)), wmul(t->C2, wsub(cy, t->v2y)));
         double rgb[3];
-        shade_pixel(f, ti, (float)e1 * t->invDet, (float)e2 * t->invDet, rgb);
+        shade_pixel(f, ti, (float)e1 * t->invDet, (float)e2 * t->invDet, x, y, rgb);
         for (int q = 0; q < 3; q++)
             acc[q] += (float)to_byte((float)rgb[q]) / 255.0f;
         acc[3] += 255.0f / 255.0f;
@@ -1045,7 +1274,7 @@ static void shade_row(frame* f, edxr_oracle_out* out, int y)
                 c[0] = c[1] = c[2] = c[3] = 0.0;
             else
             {
-                shade_pixel(f, ti, f->l0[pp], f->l1[pp], c);
+                shade_pixel(f, ti, f->l0[pp], f->l1[pp], x, y, c);
                 c[3] = 1.0;
             }
         }
@@ -1097,6 +1326,13 @@ int edxr_oracle_render(const edxr_oracle_params* P, const edxr_oracle_mesh* M, e
     f.P = P;
     f.M = M;
     int rc = -3;
+    if (P->num_textures > 0)
+    {
+        f.tex = (otex*)calloc((size_t)P->num_textures, sizeof(otex));
+        if (!f.tex) goto done;
+        for (int i = 0; i < P->num_textures; i++)
+            if (build_texture(&P->textures[i], &f.tex[i])) goto done;
+    }
     mat_mul(P->proj, P->mv, f.mvp);
     eye_position(P->mv, f.eye);
 
@@ -1156,5 +1392,10 @@ int edxr_oracle_render(const edxr_oracle_params* P, const edxr_oracle_mesh* M, e
 done:
     free(f.proj); free(f.rv); free(f.rt); free(f.refStart); free(f.refs);
     free(f.depth); free(f.win); free(f.l0); free(f.l1); free(f.tileFrags);
+    if (f.tex)
+    {
+        for (int i = 0; i < P->num_textures; i++) free(f.tex[i].texels);
+        free(f.tex);
+    }
     return rc;
 }

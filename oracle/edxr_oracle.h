@@ -30,8 +30,17 @@ enum
     EDXR_ORACLE_PS_BLINN_PHONG = 0,           /* albedo*diffuse + ks*max(N.H,0)^s */
     EDXR_ORACLE_PS_BLINN_PHONG_REFERENCE = 1, /* Shader.h:249-281: diffuse + ks*(N.H)^s */
     EDXR_ORACLE_PS_LAMBERTIAN_ALBEDO = 2,     /* Shader.h:212-243 with per-vertex albedo */
-    EDXR_ORACLE_PS_LAMBERTIAN = 3             /* Shader.h:188-206 */
+    EDXR_ORACLE_PS_LAMBERTIAN = 3,            /* Shader.h:188-206 */
+    EDXR_ORACLE_PS_LAMBERTIAN_TEXTURED = 4    /* Shader.h:209-244, albedo sampled from the texture */
 };
+
+/* One texture slot: texels in rows of `width`, row 0 at v = 0; format 0 =
+ * RGBA8 (channel = byte / 255), 1 = RGBA32F. */
+typedef struct
+{
+    int width, height, format;
+    const void* texels;
+} edxr_oracle_texture;
 
 typedef struct
 {
@@ -46,6 +55,9 @@ typedef struct
     float ks, shininess;
     int threads;      /* worker threads for the per-tile stages (>=1) */
     int msaa_log2;    /* RenderStates::MultiSampleLevel: 0 (one sample) .. 5 (32 samples) */
+    const edxr_oracle_texture* textures; /* texture slots of the textured shader */
+    int num_textures;
+    int texture_filter; /* 0 nearest, 1 linear, 2 trilinear, 3..5 anisotropic 4x/8x/16x */
 } edxr_oracle_params;
 
 typedef struct
@@ -56,6 +68,7 @@ typedef struct
     const float* albedo;    int albedo_stride;   /* may be NULL -> 1 */
     const uint32_t* indices;                     /* 3 per triangle */
     int nv, nt;
+    const uint32_t* texture_ids;                 /* per triangle, may be NULL -> 0 */
 } edxr_oracle_mesh;
 
 /* With S = 1 << msaa_log2 samples, id and depth hold S planes of W*H

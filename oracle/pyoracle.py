@@ -23,7 +23,13 @@ class _Params(ctypes.Structure):
                 ("depth_func", ctypes.c_int), ("hierarchical", ctypes.c_int),
                 ("shader", ctypes.c_int), ("light", ctypes.c_float * 3),
                 ("ks", ctypes.c_float), ("shininess", ctypes.c_float),
-                ("threads", ctypes.c_int), ("msaa_log2", ctypes.c_int)]
+                ("threads", ctypes.c_int), ("msaa_log2", ctypes.c_int),
+                ("textures", ctypes.c_void_p), ("num_textures", ctypes.c_int), ("texture_filter", ctypes.c_int)]
+
+
+class _Texture(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int), ("format", ctypes.c_int),
+                ("texels", ctypes.c_void_p)]
 
 
 class _Mesh(ctypes.Structure):
@@ -31,7 +37,8 @@ class _Mesh(ctypes.Structure):
                 ("normals", ctypes.c_void_p), ("normal_stride", ctypes.c_int),
                 ("uvs", ctypes.c_void_p), ("uv_stride", ctypes.c_int),
                 ("albedo", ctypes.c_void_p), ("albedo_stride", ctypes.c_int),
-                ("indices", ctypes.c_void_p), ("nv", ctypes.c_int), ("nt", ctypes.c_int)]
+                ("indices", ctypes.c_void_p), ("nv", ctypes.c_int), ("nt", ctypes.c_int),
+                ("texture_ids", ctypes.c_void_p)]
 
 
 class _Out(ctypes.Structure):
@@ -96,9 +103,10 @@ def make_params(view, threads=None, hierarchical=True, shader=None, depth_func=N
 
 
 def render_oracle(mesh, view, threads=None, hierarchical=True, depth_func=None, shader=None,
-                  with_color=True, msaa_log2=0):
+                  with_color=True, msaa_log2=0, textures=None, texture_filter=2):
     """Run the C restatement.  Returns a dict of numpy arrays and statistics;
-    with msaa_log2 > 0, id and depth are (samples, H, W)."""
+    with msaa_log2 > 0, id and depth are (samples, H, W).  `textures`: the
+    texture slots of the textured shader, (H, W, 4) uint8 or float32 arrays."""
     lib = _oracle_lib()
     W, H = view.width, view.height
     pos = np.ascontiguousarray(mesh.positions, np.float32)
@@ -106,8 +114,10 @@ def render_oracle(mesh, view, threads=None, hierarchical=True, depth_func=None, 
     alb = np.ascontiguousarray(mesh.albedo, np.float32)
     uv = np.ascontiguousarray(mesh.uvs, np.float32)
     idx = np.ascontiguousarray(mesh.indices, np.uint32)
+    tid = getattr(mesh, "texture_ids", None)
+    tid = None if tid is None else np.ascontiguousarray(tid, np.uint32)
     m = _Mesh(pos.ctypes.data, 3, nrm.ctypes.data, 3, uv.ctypes.data, 2, alb.ctypes.data, 3,
-              idx.ctypes.data, mesh.nv, mesh.nt)
+              idx.ctypes.data, mesh.nv, mesh.nt, _ptr(tid))
     S = 1 << msaa_log2
     shape = (H, W) if S == 1 else (S, H, W)
     out_id = np.empty(shape, np.uint32)
@@ -117,6 +127,18 @@ def render_oracle(mesh, view, threads=None, hierarchical=True, depth_func=None, 
     color = np.empty((H, W, 4), np.float64) if with_color else None
     o = _Out(out_id.ctypes.data, out_depth.ctypes.data, l0.ctypes.data, l1.ctypes.data, _ptr(color))
     p = make_params(view, threads, hierarchical, shader, depth_func, msaa_log2)
+    keep = []
+    if textures:
+        descs = []
+        for t in textures:
+            a = np.ascontiguousarray(t)
+            keep.append(a)
+            descs.append(_Texture(a.shape[1], a.shape[0], 0 if a.dtype == np.uint8 else 1, a.ctypes.data))
+        arr = (_Texture * len(descs))(*descs)
+        keep.append(arr)
+        p.textures = ctypes.cast(arr, ctypes.c_void_p)
+        p.num_textures = len(descs)
+    p.texture_filter = texture_filter
     rc = lib.edxr_oracle_render(ctypes.byref(p), ctypes.byref(m), ctypes.byref(o))
     if rc != 0:
         raise RuntimeError("oracle failed with code %d" % rc)
