@@ -54,6 +54,14 @@ class Texture(ctypes.Structure):
                 ("texels", ctypes.c_void_p)]
 
 
+class ObjMesh(ctypes.Structure):
+    _fields_ = [("num_vertices", ctypes.c_uint32), ("num_triangles", ctypes.c_uint32),
+                ("num_textures", ctypes.c_uint32),
+                ("positions", ctypes.POINTER(ctypes.c_float)), ("normals", ctypes.POINTER(ctypes.c_float)),
+                ("uvs", ctypes.POINTER(ctypes.c_float)), ("indices", ctypes.POINTER(ctypes.c_uint32)),
+                ("texture_ids", ctypes.POINTER(ctypes.c_uint32)), ("textures", ctypes.POINTER(Texture))]
+
+
 class Outputs(ctypes.Structure):
     _fields_ = [("color", ctypes.c_void_p), ("depth", ctypes.c_void_p), ("triangle_id", ctypes.c_void_p),
                 ("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("samples", ctypes.c_uint32)]
@@ -97,6 +105,8 @@ SIGNATURES = {
     "edxr_set_shader": ([_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ShaderParams)], ctypes.c_int),
     "edxr_render": ([_P, ctypes.POINTER(Mesh)], ctypes.c_int),
     "edxr_set_textures": ([_P, ctypes.POINTER(Texture), ctypes.c_uint32], ctypes.c_int),
+    "edxr_load_obj": ([ctypes.c_char_p, _P, _P, _P, ctypes.POINTER(ctypes.POINTER(ObjMesh))], ctypes.c_int),
+    "edxr_free_obj": ([ctypes.POINTER(ObjMesh)], None),
     "edxr_synchronize": ([_P], ctypes.c_int),
     "edxr_get_outputs": ([_P, ctypes.POINTER(Outputs)], ctypes.c_int),
     "edxr_read_outputs": ([_P, _P, _P, _P], ctypes.c_int),

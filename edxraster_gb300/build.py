@@ -1,6 +1,6 @@
 """Build recipe of the CUDA library ``libedxr.so`` (sm_103a only).
 
-Every ``csrc/*.cu`` translation unit is compiled in parallel with
+Every ``csrc/*.cu`` (and host-only ``csrc/*.cpp``) translation unit is compiled in parallel with
 ``nvcc -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo -fmad=false``
 (no contraction of float products into fused multiply-adds: coverage, depth
 and the winning triangle must reproduce the reference's rounding), then
@@ -34,7 +34,7 @@ def _run(cmd):
 
 
 def _sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
 def _deps():

@@ -152,7 +152,8 @@ struct edxr_renderer
     cudaStream_t stream = nullptr;
     int num_sms = 0;
     uint32_t width = 0, height = 0;
-    edxr_state state = { EDXR_DEPTH_LEQUAL, 1, 0, 0 };
+    // RenderStates::DefaultSettings (RenderStates.h:55-61): LEQUAL, hierarchical, one sample, trilinear
+    edxr_state state = { EDXR_DEPTH_LEQUAL, 1, 0, EDXR_FILTER_TRILINEAR };
     Shading shading;
     Camera cam;
 

@@ -132,7 +132,7 @@ class Renderer:
         self._device = device
         self._stream = stream
         self._width = self._height = 0
-        self._state = _lib.State(DEPTH_LEQUAL, 1, 0, 0)
+        self._state = _lib.State(DEPTH_LEQUAL, 1, 0, FILTER_TRILINEAR)  # RenderStates::DefaultSettings
         self._write_frames = False
         self._frame = 0
         self._keep = None
@@ -369,6 +369,39 @@ class Renderer:
         _lib.check(self._lib.edxr_read_batch_outputs(self._h, first, count, color.ctypes.data, depth.ctypes.data,
                                                      tid.ctypes.data))
         return color, depth, tid
+
+
+def load_obj(path: str, pos=(0.0, 0.0, 0.0), scale=(1.0, 1.0, 1.0), rot=(0.0, 0.0, 0.0)):
+    """Mesh::LoadMesh (Mesh.cpp:11-34) through edxr_load_obj: a Wavefront OBJ
+    file with its MTL materials.  Returns (scenes.Mesh with texture_ids, list of
+    (H, W, 4) float32 textures, one per material slot, slot 0 = white default)."""
+    from . import scenes
+    lib = _lib.load()
+    f3 = ctypes.c_float * 3
+    p, s, r = f3(*pos), f3(*scale), f3(*rot)
+    m = ctypes.POINTER(_lib.ObjMesh)()
+    _lib.check(lib.edxr_load_obj(os.fsencode(path), ctypes.addressof(p), ctypes.addressof(s), ctypes.addressof(r),
+                                 ctypes.byref(m)))
+    try:
+        o = m.contents
+        nv, nt = o.num_vertices, o.num_triangles
+        arr = lambda ptr, n, dt: np.ctypeslib.as_array(ptr, shape=(n,)).astype(dt).copy() if n else np.zeros(0, dt)  # noqa: E731
+        pos_ = arr(o.positions, 3 * nv, np.float32).reshape(-1, 3)
+        nrm = arr(o.normals, 3 * nv, np.float32).reshape(-1, 3)
+        uvs = arr(o.uvs, 2 * nv, np.float32).reshape(-1, 2)
+        idx = arr(o.indices, 3 * nt, np.uint32).reshape(-1, 3)
+        tid = arr(o.texture_ids, nt, np.uint32)
+        textures = []
+        for k in range(o.num_textures):
+            t = o.textures[k]
+            buf = ctypes.cast(t.texels, ctypes.POINTER(ctypes.c_float))
+            textures.append(np.ctypeslib.as_array(buf, shape=(t.height * t.width * 4,)).reshape(
+                t.height, t.width, 4).copy())
+    finally:
+        lib.edxr_free_obj(m)
+    mesh = scenes.Mesh(pos_, nrm, np.ones_like(pos_), uvs, idx)
+    mesh.texture_ids = tid
+    return mesh, textures
 
 
 def configure(r: Renderer, view, hierarchical: bool = True):

@@ -220,6 +220,33 @@ edxr_status edxr_set_shader(edxr_renderer* r, int vs_kind, int ps_kind,
  * the previous set; count 0 clears it. */
 edxr_status edxr_set_textures(edxr_renderer* r, const edxr_texture* textures, uint32_t count);
 
+/* ------------------------------------------------------------------------
+ * Mesh input (Mesh::LoadMesh, Mesh.cpp:11-34, over EDXUtil's ObjMesh, which
+ * the reference does not include): a Wavefront OBJ file with its MTL
+ * materials, loaded into host arrays ready for edxr_mesh and
+ * edxr_set_textures.  Faces are fanned into triangles; every distinct
+ * (position, texture coordinate, normal) corner becomes one vertex; missing
+ * normals are the area-weighted mean of the adjacent face normals.  The
+ * transform is scale, then rotation about x, y, z (degrees, in that order),
+ * then translation, as LoadMesh(pos, scl, rot, path) takes them.  Each
+ * material is one texture slot: its map_Kd image (binary PPM or uncompressed
+ * 24/32-bit BMP) or a 1x1 texture of its Kd colour; a triangle's texture id
+ * is the slot of its usemtl material (slot 0, white, when there is none). */
+typedef struct edxr_obj_mesh
+{
+    uint32_t num_vertices, num_triangles, num_textures;
+    float* positions;          /* num_vertices x 3                                */
+    float* normals;            /* num_vertices x 3                                */
+    float* uvs;                /* num_vertices x 2                                */
+    uint32_t* indices;         /* num_triangles x 3                               */
+    uint32_t* texture_ids;     /* num_triangles                                   */
+    edxr_texture* textures;    /* num_textures, RGBA32F texels owned by the mesh  */
+} edxr_obj_mesh;
+
+edxr_status edxr_load_obj(const char* path, const float pos[3], const float scale[3], const float rot_deg[3],
+                          edxr_obj_mesh** mesh);
+void edxr_free_obj(edxr_obj_mesh* mesh);
+
 /* Renderer::RenderMesh, Renderer.cpp:100-118: clear, then render one mesh. */
 edxr_status edxr_render(edxr_renderer* r, const edxr_mesh* mesh);
 

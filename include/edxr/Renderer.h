@@ -61,6 +61,12 @@ inline PixelShader LambertianPixelShader(float lx = 1.0f, float ly = 1.0f, float
 {
     return PixelShader{ EDXR_PS_LAMBERTIAN, { { lx, ly, lz }, 0.0f, 1.0f } };
 }
+// LambertianAlbedoPixelShader as written: the albedo is sampled from the
+// triangle's texture slot (Renderer::SetTextures, Mesh::SetTextureIds).
+inline PixelShader TexturedLambertianPixelShader(float lx = 1.0f, float ly = 1.0f, float lz = -1.0f)
+{
+    return PixelShader{ EDXR_PS_LAMBERTIAN_TEXTURED, { { lx, ly, lz }, 0.0f, 1.0f } };
+}
 
 enum class TextureFilter { Nearest, Linear, TriLinear, Anisotropic4x, Anisotropic8x, Anisotropic16x };
 
@@ -108,12 +114,26 @@ public:
         m.desc.memory = memory;
         return m;
     }
+    // Texture coordinates (two floats per vertex) and per-triangle texture
+    // slots (Mesh::GetTextureIds, Mesh.h:56-59).
+    Mesh& SetTexCoords(const float* uvs, uint32_t strideBytes = 8)
+    {
+        desc.uvs = uvs;
+        desc.uv_stride = strideBytes;
+        return *this;
+    }
+    Mesh& SetTextureIds(const uint32_t* ids)
+    {
+        desc.texture_ids = ids;
+        return *this;
+    }
 };
 
 class Renderer
 {
     edxr_renderer* mpRenderer = nullptr;
-    edxr_state mState{ EDXR_DEPTH_LEQUAL, 1, 0, 0 };
+    // RenderStates::DefaultSettings (RenderStates.h:55-61)
+    edxr_state mState{ EDXR_DEPTH_LEQUAL, 1, 0, EDXR_FILTER_TRILINEAR };
     uint32_t mWidth = 0, mHeight = 0;
     bool mWriteFrames = false;
     int mFrameCount = 0;
@@ -198,6 +218,12 @@ public:
         s.msaa_log2 = msaaCountLog2;
         edxr::Check(edxr_set_state(mpRenderer, &s));
         mState = s;
+    }
+    // Texture slots (Mesh::GetTextures / RenderStates::TextureSlots): texels
+    // copied, mip chains built on the device.
+    void SetTextures(const edxr_texture* textures, uint32_t count)
+    {
+        edxr::Check(edxr_set_textures(mpRenderer, textures, count));
     }
     void SetTextureFilter(TextureFilter filter)
     {

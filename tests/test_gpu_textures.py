@@ -80,3 +80,31 @@ def test_texture_errors(cuda_lib):
         r.SetTextureFilter(9)
     r.SetTextures([])  # clearing is allowed
     r.close()
+
+
+def test_obj_file_renders_like_the_oracle(cuda_lib, tmp_path):
+    """Mesh::LoadMesh's path: an OBJ file with MTL materials (an image texture
+    and a constant colour) loaded by edxr_load_obj and rendered textured."""
+    sc = scenes.textured_scene(160, 96)
+    m = sc.mesh
+    checker = scenes.test_textures()[0]
+    ppm = checker[::-1, :, :3]  # PPM rows run top-down; the texture's row 0 is its bottom
+    (tmp_path / "check.ppm").write_bytes(b"P6\n64 64\n255\n" + np.ascontiguousarray(ppm).tobytes())
+    (tmp_path / "scene.mtl").write_text("newmtl check\nmap_Kd check.ppm\nnewmtl warm\nKd 0.9 0.6 0.3\n")
+    lines = ["mtllib scene.mtl"]
+    lines += ["v %.9g %.9g %.9g" % tuple(p) for p in m.positions]
+    lines += ["vt %.9g %.9g" % tuple(t) for t in m.uvs]
+    lines += ["vn %.9g %.9g %.9g" % tuple(n) for n in m.normals]
+    cur = None
+    for tri, slot in zip(m.indices, m.texture_ids):
+        name = "check" if slot == 0 else "warm"
+        if name != cur:
+            lines.append("usemtl " + name)
+            cur = name
+        lines.append("f " + " ".join("%d/%d/%d" % (i + 1, i + 1, i + 1) for i in tri))
+    (tmp_path / "scene.obj").write_text("\n".join(lines) + "\n")
+    mesh, tex = R.load_obj(str(tmp_path / "scene.obj"))
+    assert mesh.nt == m.nt and len(tex) == 3
+    assert np.allclose(tex[1][..., :3], checker[..., :3] / 255.0)
+    loaded = scenes.Scene("obj", mesh, sc.view)
+    check(loaded, tex, R.FILTER_TRILINEAR)
