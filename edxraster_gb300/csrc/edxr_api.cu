@@ -402,10 +402,16 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     // reports an overflow (sync_pass renders that frame again).  The test
     // knob EDXR_DEBUG_CAPACITY starts them all tiny instead, so the first
     // frame exercises that recovery.
+    // Raster-triangle slots: one per input triangle (always), then room for
+    // the fan pieces of clipped triangles.
     if (r->debug_cap && r->rtri_cap == 0)
-        r->rtri_cap = r->poly_cap = r->big_cap = r->bin_capacity = r->debug_cap;
+    {
+        r->poly_cap = r->big_cap = r->bin_capacity = r->debug_cap;
+        r->rtri_cap = tt + r->debug_cap;
+    }
     else
-        r->rtri_cap = std::max<uint64_t>({ r->rtri_cap, tt + std::max<uint64_t>(tt / 4, 65536) });
+        r->rtri_cap = std::max<uint64_t>({ r->rtri_cap, tt + (r->debug_cap ? r->debug_cap
+                                                                           : std::max<uint64_t>(tt / 4, 65536)) });
     if (!r->debug_cap)
     {
         r->poly_cap = std::max<uint64_t>({ r->poly_cap, std::max<uint64_t>(tt / 16, 65536) });
@@ -530,7 +536,7 @@ edxr_status sync_pass(edxr_renderer* r)
         PassArgs a = r->last;
         if (st.overflow & 2u)
         {
-            r->rtri_cap = std::min<uint64_t>((uint64_t)st.raster_tris + st.raster_tris / 4 + 1024, 0xFFFFFFF0u);
+            r->rtri_cap = std::min<uint64_t>((uint64_t)st.rtri_slots + st.rtri_slots / 4 + 1024, 0xFFFFFFF0u);
             EDXR_CUDA(r->rtris.ensure(sizeof(RTri) * r->rtri_cap));
             a.rtris = r->rtris.as<RTri>();
             a.rtri_capacity = (uint32_t)r->rtri_cap;

@@ -117,7 +117,7 @@ struct DeviceStatus
     uint32_t raster_tris;    // needed (may exceed the capacity)
     uint32_t clipped_polys;  // needed
     uint32_t big_tris;       // needed
-    uint32_t pad;
+    uint32_t rtri_slots;     // raster-triangle slots needed: input triangles + fan pieces
 };
 
 // Tunables of one pass (edxr_set_tuning; chosen by the autotuner).
@@ -138,7 +138,7 @@ struct PassArgs
     uint32_t total_vertices;
     uint32_t total_tris;
     uint32_t total_tiles;
-    RTri* rtris;
+    RTri* rtris;             // slot i < total_tris: unclipped input triangle i; then fan pieces (counters[0])
     uint32_t rtri_capacity;
     ClipPoly* polys;
     uint32_t poly_capacity;  // also the capacity of clip_list
@@ -153,14 +153,14 @@ struct PassArgs
     uint32_t big_capacity;
     uint32_t* counters;      // [0] raster tris, [1] polys, [2] big tris, [3] raster work queue, [4] clip list,
                              // [5] unsorted bin list slots, [6] heavy raster work items, [7] light ones,
-                             // [8] scan block tickets (kCounters words)
+                             // [8] scan block tickets, [10] unclipped surviving triangles (kCounters words)
     unsigned long long* scan_status;  // per scan block (scan_blocks(total_tiles) words)
     uint2* items;            // raster work items (tile, index of its kItemEntries-entry slice): heavy ones
                              // from the front, light ones from the back
     uint64_t item_capacity;
     unsigned long long* keybuf;  // per pixel: ~(smallest key) of split tiles, 0 between passes
     DeviceStatus* status;
-    uint32_t* tri_first;     // per flattened input triangle: its first raster triangle (or kNoTriangle)
+    uint32_t* tri_first;     // per clipped input triangle: its first fan piece
     float4* color;
     float* depth;
     uint32_t* tri_id;        // the winner's input-triangle id (kNoTriangle: background)

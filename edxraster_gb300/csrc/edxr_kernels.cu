@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(256) k_setup(PassArgs a)
         }
         if (lane == 7)
         {
-            s_base[0] = (wi & 0xFFFFu) ? atomicAdd(&a.counters[0], wi & 0xFFFFu) : 0u;
+            s_base[0] = (wi & 0xFFFFu) ? atomicAdd(&a.counters[10], wi & 0xFFFFu) : 0u;  // survivors (statistics)
             s_base[1] = (wi >> 16) ? atomicAdd(&a.counters[4], wi >> 16) : 0u;
             s_base[2] = wei ? atomicAdd(&a.counters[5], wei) : 0u;
         }
@@ -298,29 +298,18 @@ __global__ void __launch_bounds__(256) k_setup(PassArgs a)
         if (q < a.poly_capacity)
             a.clip_list[q] = gi;
     }
-    const uint32_t base = s_base[0] + (excl & 0xFFFFu);
+    // an unclipped triangle's record sits at its flattened index
     const uint32_t slot = s_base[2] + s_went[warp] + eincl - nent;
-    const bool stored = nOut && base < a.rtri_capacity;
-    if (gi < a.total_tris)
-        a.tri_first[gi] = stored ? base : kNoTriangle;  // k_clip sets clipped ones
-    if (nOut && !stored)
-    {
-        atomicOr(&a.status->overflow, 2u);
-        // the reserved entry slots stay in the list, empty
-        for (uint32_t k = 0; k < nent; k++)
-            if (slot + k < a.bin_capacity)
-                a.bin_tmp[slot + k] = make_uint2(kEmptySlot, 0u);
-    }
-    if (stored)
+    if (nOut)
     {
         t.order = tri << 4;
         t.meta |= fi << 12;
         t.poly = kUnclipped;
-        a.rtris[base] = t;
+        a.rtris[gi] = t;
     }
-    bin_big_append(a, base, stored && big);
-    if (stored && nent)
-        bin_small(a, a.frames[fi], base, st, slot);
+    bin_big_append(a, gi, nOut && big);
+    if (nOut && nent)
+        bin_small(a, a.frames[fi], gi, st, slot);
 }
 
 // Clipping of the queued triangles (Clipper.h:107-171): Sutherland-Hodgman,
@@ -354,14 +343,16 @@ __global__ void __launch_bounds__(128) k_clip(PassArgs a)
                 nOut += setup_triangle(f, vc[0], vc[k - 1], vc[k], tmp) ? 1 : 0;
             }
         }
+        // the fan pieces follow all input-triangle slots
         uint32_t out = warp_append(&a.counters[0], nOut);
         if (nOut == 0)
             continue;
-        if (out + (uint32_t)nOut > a.rtri_capacity)
+        if ((uint64_t)a.total_tris + out + (uint32_t)nOut > a.rtri_capacity)
         {
             atomicOr(&a.status->overflow, 2u);
             continue;
         }
+        out += a.total_tris;
         const FrameDesc& f = a.frames[fi];
         // one polygon record per lane with output, one atomic per warp
         const uint32_t act = __activemask();
@@ -383,14 +374,15 @@ __global__ void __launch_bounds__(128) k_clip(PassArgs a)
             P.w[j][2] = poly[j].w2;
         }
         P.n = (uint32_t)n;
-        // the surviving fan triangles are contiguous and in fan order
+        // the surviving fan triangles are contiguous and in fan order; their
+        // fan field counts from 1, so 0 marks a triangle that was not clipped
         a.tri_first[gi] = out;
         for (int k = 2; k < n; k++)
         {
             RTri tk;
             if (!setup_triangle(f, vc[0], vc[k - 1], vc[k], tk))
                 continue;
-            tk.order = (tri << 4) | (uint32_t)(k - 2);
+            tk.order = (tri << 4) | (uint32_t)(k - 1);
             tk.meta |= fi << 12;
             tk.poly = (pi << 4) | (uint32_t)k;
             a.rtris[out] = tk;
@@ -720,9 +712,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
         // the unsorted list shares the capacity
         const uint64_t needed = max(grand, (uint64_t)a.counters[5]);
         a.status->bins_needed = needed;
-        a.status->raster_tris = a.counters[0];
+        a.status->raster_tris = a.counters[10] + a.counters[0];
+        a.status->rtri_slots = a.total_tris + a.counters[0];
         a.status->big_tris = a.counters[2];
-        if (a.counters[0] > a.rtri_capacity)
+        if ((uint64_t)a.total_tris + a.counters[0] > a.rtri_capacity)
             atomicOr(&a.status->overflow, 2u);
         if (a.counters[1] > a.poly_capacity || a.counters[4] > a.poly_capacity)
             atomicOr(&a.status->overflow, 4u);
@@ -890,17 +883,18 @@ struct __align__(16) StagedSlot
 };
 
 // Raster triangle of the fragment with submission rank `rank` (0: none), or
-// kNoTriangle.  rank - 1 = flattened input triangle * 16 + fan index; the
-// fan pieces of a clipped triangle are contiguous, in fan order, from
-// tri_first.
+// kNoTriangle.  rank - 1 = flattened input triangle * 16 + fan field: 0 for a
+// triangle that was not clipped, whose record sits at its flattened index;
+// piece k - 1 of a clipped triangle otherwise, found from tri_first (the
+// pieces are contiguous, in fan order).
 __device__ __forceinline__ uint32_t raster_triangle_of(const PassArgs& a, uint32_t rank, uint32_t nr)
 {
     if (rank == 0)
         return kNoTriangle;
     const uint32_t gi = (rank - 1u) >> 4, fan = (rank - 1u) & 15u;
-    uint32_t ri = gi < a.total_tris ? a.tri_first[gi] : kNoTriangle;
     if (fan == 0)
-        return ri < nr ? ri : kNoTriangle;
+        return gi < a.total_tris ? gi : kNoTriangle;
+    uint32_t ri = gi < a.total_tris ? a.tri_first[gi] : kNoTriangle;
     for (int s = 0; s < kMaxPolygon && ri < nr && (a.rtris[ri].order & 15u) != fan; s++)
         ri++;
     return (ri < nr && (a.rtris[ri].order & 15u) == fan) ? ri : kNoTriangle;
@@ -959,7 +953,9 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long* key = s_key[warp];
     StagedSlot* staged = s_tri[warp];
-    const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
+    // raster-triangle slots in use: one per input triangle, then the fan pieces
+    const uint32_t nr = (uint32_t)min((uint64_t)a.total_tris + *(volatile uint32_t*)&a.counters[0],
+                                      (uint64_t)a.rtri_capacity);
     const uint32_t nheavy = *(volatile uint32_t*)&a.counters[6];
     const uint32_t nitems = (uint32_t)min((uint64_t)nheavy + *(volatile uint32_t*)&a.counters[7], a.item_capacity);
     const int small_region = min(a.tune.small_region, 64);
@@ -1281,7 +1277,9 @@ __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
     StagedTri* staged = reinterpret_cast<StagedTri*>(key + 256 * S);            // 32 x 64 bytes
     int* sg = reinterpret_cast<int*>(key + 256 * S + 32 * 8);                    // 32 x 3 ints (G)
     const int level = a.msaa_log2;
-    const uint32_t nr = min(*(volatile uint32_t*)&a.counters[0], a.rtri_capacity);
+    // raster-triangle slots in use: one per input triangle, then the fan pieces
+    const uint32_t nr = (uint32_t)min((uint64_t)a.total_tris + *(volatile uint32_t*)&a.counters[0],
+                                      (uint64_t)a.rtri_capacity);
     const uint32_t nheavy = *(volatile uint32_t*)&a.counters[6];
     const uint32_t nitems = (uint32_t)min((uint64_t)nheavy + *(volatile uint32_t*)&a.counters[7], a.item_capacity);
     const uint64_t plane = a.total_pixels;
