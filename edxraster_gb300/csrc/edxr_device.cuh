@@ -464,9 +464,16 @@ __device__ __forceinline__ float3 lerp3(float b0, float3 a, float b1, float3 b, 
     return f3(fmaf(b0, a.x, fmaf(b1, b.x, b2 * c.x)), fmaf(b0, a.y, fmaf(b1, b.y, b2 * c.y)),
               fmaf(b0, a.z, fmaf(b1, b.z, b2 * c.z)));
 }
+// 1/sqrt(x) from the hardware estimate refined by one Newton step (relative
+// error a few 1e-8, well inside the 1e-5 colour tolerance).
+__device__ __forceinline__ float rsqrt_nr(float x)
+{
+    const float y = rsqrtf(x);
+    return y * fmaf(-0.5f * x * y, y, 1.5f);
+}
 __device__ __forceinline__ float3 normalize3(float3 v)
 {
-    const float inv = 1.0f / sqrtf(dot3(v, v));
+    const float inv = rsqrt_nr(dot3(v, v));
     return f3(v.x * inv, v.y * inv, v.z * inv);
 }
 __device__ __forceinline__ float3 ld3(const char* base, uint32_t stride, uint32_t i, float dflt)
@@ -543,7 +550,9 @@ __device__ __forceinline__ float3 shade_model(const FrameDesc& f, float3 P, floa
         float nh = dot3(N, H);
         if (f.ps_kind == 0)
             nh = fmaxf(nh, 0.0f);
-        spec = f.ks * powf(nh, f.shininess);
+        // nh^shininess as 2^(shininess log2 nh) (nh is clamped to >= 0 here:
+        // log2 0 = -inf gives 0; the unclamped reference shader shades in FP64)
+        spec = f.ks * exp2f(f.shininess * log2f(nh));
     }
     switch (f.ps_kind)
     {
@@ -791,7 +800,7 @@ __device__ __forceinline__ float3 shade_fragment(const FrameDesc& f, const RTri&
     b0 = fmul(b0, t.invW0);
     b1 = fmul(b1, t.invW1);
     b2 = fmul(b2, t.invW2);
-    const float invB = fdiv(1.0f, fadd(fadd(b0, b1), b2));
+    const float invB = __frcp_rn(fadd(fadd(b0, b1), b2));
     b0 = fmul(b0, invB);
     b1 = fmul(b1, invB);
     b2 = fsub(fsub(1.0f, b0), b1);
