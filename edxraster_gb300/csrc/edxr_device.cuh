@@ -153,44 +153,6 @@ __device__ __forceinline__ PolyVert plane_cut(int plane, const PolyVert& a, cons
     return r;
 }
 
-// Clipper::ClipPolygon (Clipper.h:235-288): Sutherland-Hodgman against the
-// planes in planeCode, in the order L, R, B, T, F, N, then the polygon is
-// dropped when any vertex has w <= 0.  Returns the vertex count.
-static __device__ __noinline__ int clip_polygon(PolyVert* poly, uint32_t planeCode)
-{
-    PolyVert tmp[kMaxPolygon];
-    int n = 3;
-    const uint32_t bits[6] = { kLeft, kRight, kBottom, kTop, kFar, kNear };
-    for (int k = 0; k < 6; k++)
-    {
-        if (!(planeCode & bits[k]))
-            continue;
-        int m = 0;
-        for (int i = 0; i < n; i++)
-        {
-            const int i1 = (i + 1 == n) ? 0 : i + 1;
-            const bool in0 = plane_inside(k, poly[i].p);
-            const bool in1 = plane_inside(k, poly[i1].p);
-            if (in0)
-            {
-                if (m < kMaxPolygon) tmp[m++] = in1 ? poly[i1] : plane_cut(k, poly[i], poly[i1]);
-            }
-            else if (in1)
-            {
-                if (m < kMaxPolygon) tmp[m++] = plane_cut(k, poly[i], poly[i1]);
-                if (m < kMaxPolygon) tmp[m++] = poly[i1];
-            }
-        }
-        for (int i = 0; i < m; i++)
-            poly[i] = tmp[i];
-        n = m;
-    }
-    for (int i = 0; i < n; i++)
-        if (poly[i].p.w <= 0.0f)
-            return 0;
-    return n;
-}
-
 // Reject / accept corner of one edge from the sign of B / float(C) and of C
 // (RasterTriangle.h:66-150); packed as rej | acc << 2.  The quotient of two
 // converted ints is never rounded to zero and keeps the sign of B*C, so

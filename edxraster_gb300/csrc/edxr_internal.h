@@ -151,9 +151,10 @@ struct PassArgs
     uint64_t bin_capacity;
     uint32_t* big_list;      // raster triangles with many tiles, binned by whole blocks
     uint32_t big_capacity;
-    uint32_t* counters;      // [0] raster tris, [1] polys, [2] big tris, [3] raster work queue, [4] clip list,
+    uint32_t* counters;      // [0] fan-piece slots, [1] polys, [2] big tris, [3] raster work queue, [4] clip list,
                              // [5] unsorted bin list slots, [6] heavy raster work items, [7] light ones,
-                             // [8] scan block tickets, [10] unclipped surviving triangles (kCounters words)
+                             // [8] scan block tickets, [10] unclipped surviving triangles,
+                             // [11] surviving fan pieces (kCounters words)
     unsigned long long* scan_status;  // per scan block (scan_blocks(total_tiles) words)
     uint2* items;            // raster work items (tile, index of its kItemEntries-entry slice): heavy ones
                              // from the front, light ones from the back

@@ -138,37 +138,6 @@ __device__ __forceinline__ float4 clip_position(const FrameDesc& f, uint32_t v)
     return xform_point4(f.mvp, __ldg(p), __ldg(p + 1), __ldg(p + 2));
 }
 
-// -------------------------------------------------------------------------
-// Clipping + setup: one thread per input triangle.  Surviving triangles are
-// appended with a warp-aggregated atomic; each carries its submission order.
-__device__ __forceinline__ void clip_triangle(const FrameDesc& f, float4 c0, float4 c1, float4 c2,
-                                              uint32_t planes, PolyVert* poly, int& n, float4* vclip)
-{
-    poly[0] = { c0, 1.f, 0.f, 0.f };
-    poly[1] = { c1, 0.f, 1.f, 0.f };
-    poly[2] = { c2, 0.f, 0.f, 1.f };
-    n = clip_polygon(poly, planes);
-    // Clipper.h:121-152: a vertex whose weight is exactly one on a source
-    // vertex is that source vertex (position and attributes); others are new.
-    const float4 src[3] = { c0, c1, c2 };
-    for (int j = 0; j < n; j++)
-    {
-        int s = -1;
-        if (poly[j].w0 == 1.0f) s = 0;
-        else if (poly[j].w1 == 1.0f) s = 1;
-        else if (poly[j].w2 == 1.0f) s = 2;
-        if (s >= 0)
-        {
-            poly[j].w0 = (s == 0) ? 1.f : 0.f;
-            poly[j].w1 = (s == 1) ? 1.f : 0.f;
-            poly[j].w2 = (s == 2) ? 1.f : 0.f;
-            vclip[j] = src[s];
-        }
-        else
-            vclip[j] = poly[j].p;
-    }
-}
-
 // Appends n raster triangles for this lane with one atomic per warp; returns
 // the lane's first slot.  Every lane of the warp must call it.
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, int n)
@@ -313,20 +282,293 @@ __global__ void __launch_bounds__(256) k_setup(PassArgs a)
 }
 
 // Clipping of the queued triangles (Clipper.h:107-171): Sutherland-Hodgman,
-// fan triangulation, setup of each fan triangle.  Grid-stride over the queue.
-__global__ void __launch_bounds__(128) k_clip(PassArgs a)
+// fan triangulation, setup of each fan triangle.  Each clipped triangle
+// reserves n - 2 consecutive raster-triangle slots, fan piece k - 1 (fan
+// vertices 0, k - 1, k) in slot first + k - 2; a piece that setup culls
+// leaves its slot unused.  Its polygon record is the one of its queue
+// position.  Two ways to spread the work over the lanes, chosen by the
+// queue length (the kernel is latency-bound either way):
+//  - short queues (one round of the grid's 16-lane groups): a group clips
+//    one triangle with one polygon vertex per lane (a polygon has at most
+//    kMaxPolygon = 16 vertices), so the polygon stays in registers: per
+//    plane each lane classifies its edge (its vertex and the next), emits 0,
+//    1 or 2 vertices, and a scan over the group places them in the order of
+//    the serial loop (Clipper::ClipPolygon, Clipper.h:235-288);
+//  - long queues: the first `per` lanes of a warp (per <= kClipPer) clip one
+//    triangle each with the serial loop, and the warp's fan pieces are then
+//    set up one per lane.
+constexpr int kClipThreads = 128;
+constexpr int kClipWarps = kClipThreads / 32;
+constexpr int kClipLanes = 16;
+constexpr int kClipPer = 8;
+static_assert(kClipLanes == kMaxPolygon, "one lane per polygon vertex");
+
+// Bit of plane k in the order L, R, B, T, F, N.
+__device__ __forceinline__ uint32_t plane_bit(int k)
 {
-    const uint32_t nq = min(*(volatile uint32_t*)&a.counters[4], a.poly_capacity);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounds = (nq + stride - 1) / stride;
+    return k < 4 ? 1u << k : (k == 4 ? (uint32_t)kFar : (uint32_t)kNear);
+}
+
+// Clipper::ClipPolygon (Clipper.h:235-288), one lane: Sutherland-Hodgman
+// against the planes in planeCode, in the order L, R, B, T, F, N, then the
+// polygon is dropped when any vertex has w <= 0.  The polygon starts in buf0
+// and alternates between buf0 and buf1; returns the vertex count and sets
+// res to the buffer that holds the result.
+__device__ __forceinline__ int clip_polygon(PolyVert* buf0, PolyVert* buf1, uint32_t planeCode, PolyVert*& res)
+{
+    PolyVert* src = buf0;
+    PolyVert* dst = buf1;
+    int n = 3;
+#pragma unroll 1
+    for (int k = 0; k < 6; k++)
+    {
+        if (!(planeCode & plane_bit(k)))
+            continue;
+        int m = 0;
+        // edges (i, i + 1) from i = 0, the first vertex carried in registers
+        PolyVert v0 = src[0];
+        bool in0 = plane_inside(k, v0.p);
+        for (int i = 0; i < n; i++)
+        {
+            const PolyVert v1 = src[(i + 1 == n) ? 0 : i + 1];
+            const bool in1 = plane_inside(k, v1.p);
+            if (in0)
+            {
+                if (m < kMaxPolygon) dst[m++] = in1 ? v1 : plane_cut(k, v0, v1);
+            }
+            else if (in1)
+            {
+                if (m < kMaxPolygon) dst[m++] = plane_cut(k, v0, v1);
+                if (m < kMaxPolygon) dst[m++] = v1;
+            }
+            v0 = v1;
+            in0 = in1;
+        }
+        PolyVert* t = src;
+        src = dst;
+        dst = t;
+        n = m;
+    }
+    res = src;
+    for (int i = 0; i < n; i++)
+        if (src[i].p.w <= 0.0f)
+            return 0;
+    return n;
+}
+
+// Clipper.h:121-152: a polygon vertex whose weight is exactly one on a source
+// vertex is that source vertex (position and attributes); the others are
+// new.  Returns the source index, or -1, and makes the weights exact.
+__device__ __forceinline__ int source_vertex(PolyVert& v)
+{
+    int sv = -1;
+    if (v.w0 == 1.0f) sv = 0;
+    else if (v.w1 == 1.0f) sv = 1;
+    else if (v.w2 == 1.0f) sv = 2;
+    if (sv >= 0)
+    {
+        v.w0 = (sv == 0) ? 1.f : 0.f;
+        v.w1 = (sv == 1) ? 1.f : 0.f;
+        v.w2 = (sv == 2) ? 1.f : 0.f;
+    }
+    return sv;
+}
+
+// Slots of a warp's fan pieces and the capacity checks: `pieces` is this
+// lane's count (0 for lanes that hold no triangle); returns its first slot
+// and clears `pieces` when a capacity is exceeded.
+__device__ __forceinline__ uint32_t reserve_pieces(const PassArgs& a, int& pieces, uint32_t q)
+{
+    const uint32_t first = a.total_tris + warp_append(&a.counters[0], pieces);
+    if (pieces && (uint64_t)first + (uint32_t)pieces > a.rtri_capacity)
+    {
+        atomicOr(&a.status->overflow, 2u);
+        pieces = 0;
+    }
+    if (pieces && q >= a.poly_capacity)
+    {
+        atomicOr(&a.status->overflow, 4u);
+        pieces = 0;
+    }
+    return first;
+}
+
+// Setup and binning of one fan piece (c0, c1, c2 in clip space): piece `fan`
+// of input triangle `tri` of frame fi, clipped polygon `poly`, slot ri.
+// Every lane of the warp calls it; lanes with has == false hold no piece.
+__device__ __forceinline__ void clip_piece(const PassArgs& a, bool has, uint32_t fi, uint32_t tri, uint32_t poly,
+                                           uint32_t fan, uint32_t ri, float4 c0, float4 c1, float4 c2)
+{
+    const FrameDesc& f = a.frames[fi];
+    bool big = false, kept = false;
+    uint32_t nent = 0;
+    SmallTiles st;
+    RTri tk;
+    if (has && setup_triangle(f, c0, c1, c2, tk))
+    {
+        tk.order = (tri << 4) | fan;
+        tk.meta |= fi << 12;
+        tk.poly = (poly << 4) | (fan + 1u);
+        kept = true;
+        a.rtris[ri] = tk;
+        const BinGeom bg = bin_geom(tk, f);
+        big = !bg.small;
+        if (bg.small)
+            nent = small_tiles(a, f, tk, bg, st);
+    }
+    const uint32_t kept_lanes = __ballot_sync(0xffffffffu, kept);
+    if ((threadIdx.x & 31) == 0 && kept_lanes)
+        atomicAdd(&a.counters[11], (uint32_t)__popc(kept_lanes));
+    bin_big_append(a, ri, big);
+    const uint32_t slot = warp_append(&a.counters[5], (int)nent);
+    if (nent)
+        bin_small(a, f, ri, st, slot);
+}
+
+// Vertex of lane `src` (within the 16-lane group) of every lane's group.
+__device__ __forceinline__ PolyVert shfl_vert(const PolyVert& v, int src)
+{
+    PolyVert r;
+    r.p.x = __shfl_sync(0xffffffffu, v.p.x, src, kClipLanes);
+    r.p.y = __shfl_sync(0xffffffffu, v.p.y, src, kClipLanes);
+    r.p.z = __shfl_sync(0xffffffffu, v.p.z, src, kClipLanes);
+    r.p.w = __shfl_sync(0xffffffffu, v.p.w, src, kClipLanes);
+    r.w0 = __shfl_sync(0xffffffffu, v.w0, src, kClipLanes);
+    r.w1 = __shfl_sync(0xffffffffu, v.w1, src, kClipLanes);
+    r.w2 = __shfl_sync(0xffffffffu, v.w2, src, kClipLanes);
+    return r;
+}
+__device__ __forceinline__ float4 shfl_f4(float4 v, int src)
+{
+    return make_float4(__shfl_sync(0xffffffffu, v.x, src, kClipLanes), __shfl_sync(0xffffffffu, v.y, src, kClipLanes),
+                       __shfl_sync(0xffffffffu, v.z, src, kClipLanes), __shfl_sync(0xffffffffu, v.w, src, kClipLanes));
+}
+
+// Short queues: one 16-lane group per triangle, q < nq <= the grid's groups.
+__device__ __forceinline__ void clip_groups(const PassArgs& a, uint32_t nq)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const int g = (int)(lane & 15u);  // vertex lane within the group
+    const uint32_t gmask = 0xFFFFu << (lane & 16u);
+    const uint32_t q = (blockIdx.x * kClipThreads + threadIdx.x) / kClipLanes;
+    uint32_t gi = 0, fi = 0, tri = 0, code = 0;
+    PolyVert v = { make_float4(0.f, 0.f, 0.f, 0.f), 0.f, 0.f, 0.f };
+    int n = 0;
+    if (q < nq)
+    {
+        gi = a.clip_list[q];
+        fi = find_frame(a.frames, a.num_frames, gi, [](const FrameDesc& f) { return f.tri_base; });
+        const FrameDesc& f = a.frames[fi];
+        tri = gi - f.tri_base;
+        n = 3;
+        if (g < 3)
+        {
+            v.p = clip_position(f, __ldg(f.indices + 3 * (size_t)tri + g));
+            v.w0 = g == 0 ? 1.f : 0.f;
+            v.w1 = g == 1 ? 1.f : 0.f;
+            v.w2 = g == 2 ? 1.f : 0.f;
+            code = clip_code(v.p);
+        }
+    }
+    const float4 src = v.p;  // source vertex g (g < 3)
+    const uint32_t k0 = __shfl_sync(0xffffffffu, code, 0, kClipLanes);
+    const uint32_t k1 = __shfl_sync(0xffffffffu, code, 1, kClipLanes);
+    const uint32_t k2 = __shfl_sync(0xffffffffu, code, 2, kClipLanes);
+    const uint32_t planes = (k0 ^ k1) | (k1 ^ k2) | (k2 ^ k0);
+    const uint32_t any = __reduce_or_sync(0xffffffffu, planes);
+#pragma unroll 1
+    for (int k = 0; k < 6; k++)
+    {
+        const uint32_t bit = plane_bit(k);
+        if (!(any & bit))
+            continue;
+        // edge (g, g + 1 mod n): its end vertex, the cut, the emissions
+        const PolyVert v1 = shfl_vert(v, (g + 1 >= n) ? 0 : g + 1);
+        const bool valid = g < n;
+        const bool in0 = valid && plane_inside(k, v.p);
+        const bool in1 = valid && plane_inside(k, v1.p);
+        const int c = !valid ? 0 : (in0 ? 1 : (in1 ? 2 : 0));
+        PolyVert e0 = v1;
+        if (valid && in0 != in1)
+            e0 = plane_cut(k, v, v1);
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < kClipLanes; o <<= 1)
+        {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o, kClipLanes);
+            if (g >= o) incl += t;
+        }
+        const int m = min(__shfl_sync(0xffffffffu, incl, kClipLanes - 1, kClipLanes), kMaxPolygon);
+        // output vertex g: emission g - excl(s) of the first lane s whose
+        // inclusive count exceeds g
+        int s = 0;
+#pragma unroll
+        for (int st = kClipLanes / 2; st >= 1; st >>= 1)
+        {
+            const int t = __shfl_sync(0xffffffffu, incl, s + st - 1, kClipLanes);
+            if (t <= g) s += st;
+        }
+        const int which = g - __shfl_sync(0xffffffffu, incl - c, s, kClipLanes);
+        const PolyVert first = shfl_vert(e0, s);
+        const PolyVert second = shfl_vert(v1, s);
+        if (planes & bit)
+        {
+            if (g < m)
+                v = which == 0 ? first : second;
+            n = m;
+        }
+    }
+    // the polygon is dropped when any vertex has w <= 0
+    if (__ballot_sync(0xffffffffu, g < n && v.p.w <= 0.0f) & gmask)
+        n = 0;
+    const int sv = source_vertex(v);
+    const float4 sp = shfl_f4(src, sv < 0 ? 0 : sv);
+    if (sv >= 0)
+        v.p = sp;
+    int pieces = (g == 0 && n >= 3) ? n - 2 : 0;
+    const uint32_t first = __shfl_sync(0xffffffffu, reserve_pieces(a, pieces, q), 0, kClipLanes);
+    pieces = __shfl_sync(0xffffffffu, pieces, 0, kClipLanes);
+    if (pieces)
+    {
+        ClipPoly& P = a.polys[q];
+        if (g < n)
+        {
+            P.w[g][0] = v.w0;
+            P.w[g][1] = v.w1;
+            P.w[g][2] = v.w2;
+        }
+        if (g == 0)
+        {
+            P.n = (uint32_t)n;
+            a.tri_first[gi] = first;
+        }
+    }
+    // lane g: piece g + 1, fan vertices 0, g + 1, g + 2
+    const float4 f0 = shfl_f4(v.p, 0);
+    const float4 f1 = shfl_f4(v.p, min(g + 1, kClipLanes - 1));
+    const float4 f2 = shfl_f4(v.p, min(g + 2, kClipLanes - 1));
+    clip_piece(a, g < pieces, fi, tri, q, (uint32_t)g + 1u, first + (uint32_t)g, f0, f1, f2);
+}
+
+// Long queues: `per` triangles per warp and round, clipped by one lane each.
+__device__ __forceinline__ void clip_lanes(const PassArgs& a, uint32_t nq, float4 (*s_vc)[kMaxPolygon])
+{
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t nwarps = gridDim.x * kClipWarps;
+    uint32_t per = 1;
+    while (per < (uint32_t)kClipPer && (uint64_t)per * nwarps < nq)
+        per <<= 1;
+    const uint64_t span = (uint64_t)per * nwarps;
+    const uint32_t rounds = (uint32_t)((nq + span - 1) / span);
     for (uint32_t r = 0; r < rounds; r++)
     {
-        const uint32_t q = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        PolyVert poly[kMaxPolygon];
-        float4 vc[kMaxPolygon];
-        int n = 0, nOut = 0;
+        const uint64_t q64 = ((uint64_t)r * nwarps + blockIdx.x * kClipWarps + warp) * per + lane;
+        const uint32_t q = (uint32_t)min(q64, (uint64_t)0xFFFFFFFFu);
+        PolyVert buf0[kMaxPolygon], buf1[kMaxPolygon];
+        PolyVert* poly = buf0;
+        int n = 0;
         uint32_t gi = 0, fi = 0, tri = 0;
-        if (q < nq)
+        if (lane < per && q64 < nq)
         {
             gi = a.clip_list[q];
             fi = find_frame(a.frames, a.num_frames, gi, [](const FrameDesc& f) { return f.tri_base; });
@@ -336,65 +578,80 @@ __global__ void __launch_bounds__(128) k_clip(PassArgs a)
             const float4 c1 = clip_position(f, __ldg(f.indices + 3 * (size_t)tri + 1));
             const float4 c2 = clip_position(f, __ldg(f.indices + 3 * (size_t)tri + 2));
             const uint32_t k0 = clip_code(c0), k1 = clip_code(c1), k2 = clip_code(c2);
-            clip_triangle(f, c0, c1, c2, (k0 ^ k1) | (k1 ^ k2) | (k2 ^ k0), poly, n, vc);
-            for (int k = 2; k < n; k++)
+            buf0[0] = { c0, 1.f, 0.f, 0.f };
+            buf0[1] = { c1, 0.f, 1.f, 0.f };
+            buf0[2] = { c2, 0.f, 0.f, 1.f };
+            n = clip_polygon(buf0, buf1, (k0 ^ k1) | (k1 ^ k2) | (k2 ^ k0), poly);
+            const float4 src[3] = { c0, c1, c2 };
+            for (int j = 0; j < n; j++)
             {
-                RTri tmp;
-                nOut += setup_triangle(f, vc[0], vc[k - 1], vc[k], tmp) ? 1 : 0;
+                const int sv = source_vertex(poly[j]);
+                s_vc[lane][j] = sv >= 0 ? src[sv] : poly[j].p;
             }
         }
-        // the fan pieces follow all input-triangle slots
-        uint32_t out = warp_append(&a.counters[0], nOut);
-        if (nOut == 0)
-            continue;
-        if ((uint64_t)a.total_tris + out + (uint32_t)nOut > a.rtri_capacity)
+        int pieces = n >= 3 ? n - 2 : 0;
+        const uint32_t first = reserve_pieces(a, pieces, q);
+        if (pieces)
         {
-            atomicOr(&a.status->overflow, 2u);
-            continue;
+            ClipPoly& P = a.polys[q];
+            for (int j = 0; j < n; j++)
+            {
+                P.w[j][0] = poly[j].w0;
+                P.w[j][1] = poly[j].w1;
+                P.w[j][2] = poly[j].w2;
+            }
+            P.n = (uint32_t)n;
+            a.tri_first[gi] = first;
         }
-        out += a.total_tris;
-        const FrameDesc& f = a.frames[fi];
-        // one polygon record per lane with output, one atomic per warp
-        const uint32_t act = __activemask();
-        const int first = __ffs(act) - 1;
-        uint32_t pi = 0;
-        if ((int)(threadIdx.x & 31) == first)
-            pi = atomicAdd(&a.counters[1], (uint32_t)__popc(act));
-        pi = __shfl_sync(act, pi, first) + (uint32_t)__popc(act & ((1u << (threadIdx.x & 31)) - 1u));
-        if (pi >= a.poly_capacity)
+        // the warp's pieces, numbered across its lanes and taken 32 at a time
+        int incl = pieces;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
         {
-            atomicOr(&a.status->overflow, 4u);
-            continue;
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += v;
         }
-        ClipPoly& P = a.polys[pi];
-        for (int j = 0; j < n; j++)
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
+        for (int base = 0; base < total; base += 32)
         {
-            P.w[j][0] = poly[j].w0;
-            P.w[j][1] = poly[j].w1;
-            P.w[j][2] = poly[j].w2;
+            const int p = base + (int)lane;
+            // owner: the first lane whose inclusive count exceeds p
+            int j = 0;
+#pragma unroll
+            for (int st = 16; st >= 1; st >>= 1)
+            {
+                const int v = __shfl_sync(0xffffffffu, incl, j + st - 1);
+                if (v <= p) j += st;
+            }
+            const int k = p - __shfl_sync(0xffffffffu, incl - pieces, j) + 2;
+            const uint32_t jfirst = __shfl_sync(0xffffffffu, first, j);
+            const uint32_t jfi = __shfl_sync(0xffffffffu, fi, j);
+            const uint32_t jtri = __shfl_sync(0xffffffffu, tri, j);
+            const uint32_t jq = __shfl_sync(0xffffffffu, q, j);
+            const bool has = p < total;
+            const float4* vj = s_vc[j & (kClipPer - 1)];
+            float4 c0 = make_float4(0.f, 0.f, 0.f, 1.f), c1 = c0, c2 = c0;
+            if (has)
+            {
+                c0 = vj[0];
+                c1 = vj[k - 1];
+                c2 = vj[k];
+            }
+            clip_piece(a, has, jfi, jtri, jq, (uint32_t)(k - 1), jfirst + (uint32_t)(k - 2), c0, c1, c2);
         }
-        P.n = (uint32_t)n;
-        // the surviving fan triangles are contiguous and in fan order; their
-        // fan field counts from 1, so 0 marks a triangle that was not clipped
-        a.tri_first[gi] = out;
-        for (int k = 2; k < n; k++)
-        {
-            RTri tk;
-            if (!setup_triangle(f, vc[0], vc[k - 1], vc[k], tk))
-                continue;
-            tk.order = (tri << 4) | (uint32_t)(k - 1);
-            tk.meta |= fi << 12;
-            tk.poly = (pi << 4) | (uint32_t)k;
-            a.rtris[out] = tk;
-            const BinGeom g = bin_geom(tk, f);
-            bin_big_append(a, out, !g.small);
-            SmallTiles st;
-            const uint32_t nent = g.small ? small_tiles(a, f, tk, g, st) : 0u;
-            if (nent)
-                bin_small(a, f, out, st, atomicAdd(&a.counters[5], nent));
-            out++;
-        }
+        __syncwarp();
     }
+}
+
+__global__ void __launch_bounds__(kClipThreads) k_clip(PassArgs a)
+{
+    __shared__ float4 s_vc[kClipWarps][kClipPer][kMaxPolygon];
+    const uint32_t nq = min(*(volatile uint32_t*)&a.counters[4], a.poly_capacity);
+    if (nq <= gridDim.x * (uint32_t)(kClipThreads / kClipLanes))
+        clip_groups(a, nq);
+    else
+        clip_lanes(a, nq, s_vc[threadIdx.x >> 5]);
 }
 
 // Scatter of the unsorted entries into their bins (after the scan); empty
@@ -712,7 +969,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
         // the unsorted list shares the capacity
         const uint64_t needed = max(grand, (uint64_t)a.counters[5]);
         a.status->bins_needed = needed;
-        a.status->raster_tris = a.counters[10] + a.counters[0];
+        a.status->raster_tris = a.counters[10] + a.counters[11];
         a.status->rtri_slots = a.total_tris + a.counters[0];
         a.status->big_tris = a.counters[2];
         if ((uint64_t)a.total_tris + a.counters[0] > a.rtri_capacity)
@@ -885,8 +1142,8 @@ struct __align__(16) StagedSlot
 // Raster triangle of the fragment with submission rank `rank` (0: none), or
 // kNoTriangle.  rank - 1 = flattened input triangle * 16 + fan field: 0 for a
 // triangle that was not clipped, whose record sits at its flattened index;
-// piece k - 1 of a clipped triangle otherwise, found from tri_first (the
-// pieces are contiguous, in fan order).
+// piece `fan` of a clipped triangle otherwise, in slot tri_first + fan - 1
+// (each clipped triangle reserves a slot per fan piece, in fan order).
 __device__ __forceinline__ uint32_t raster_triangle_of(const PassArgs& a, uint32_t rank, uint32_t nr)
 {
     if (rank == 0)
@@ -894,10 +1151,8 @@ __device__ __forceinline__ uint32_t raster_triangle_of(const PassArgs& a, uint32
     const uint32_t gi = (rank - 1u) >> 4, fan = (rank - 1u) & 15u;
     if (fan == 0)
         return gi < a.total_tris ? gi : kNoTriangle;
-    uint32_t ri = gi < a.total_tris ? a.tri_first[gi] : kNoTriangle;
-    for (int s = 0; s < kMaxPolygon && ri < nr && (a.rtris[ri].order & 15u) != fan; s++)
-        ri++;
-    return (ri < nr && (a.rtris[ri].order & 15u) == fan) ? ri : kNoTriangle;
+    const uint32_t ri = gi < a.total_tris ? a.tri_first[gi] + fan - 1u : kNoTriangle;
+    return ri < nr ? ri : kNoTriangle;
 }
 
 // The one write of a pixel (Renderer::FragmentProcessing / UpdateFrameBuffer,
@@ -1525,7 +1780,7 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
     if (a.total_tris)
     {
         k_setup<<<(a.total_tris + 255) / 256, 256, 0, s>>>(a);
-        k_clip<<<sms * 4, 128, 0, s>>>(a);
+        k_clip<<<sms * 8, kClipThreads, 0, s>>>(a);
     }
     k_bin_big<<<sms * 4, 256, 0, s>>>(a);
     mark(2);
