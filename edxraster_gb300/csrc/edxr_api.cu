@@ -159,7 +159,7 @@ struct edxr_renderer
 
     DevBuf frames, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, bins, bin_tmp, big_list, counters,
         status;
-    DevBuf color, depth, tri_id, back8, diff_scratch, tri_first, items, keybuf;
+    DevBuf color, depth, tri_id, back8, diff_scratch, tri_first, items, keybuf, vrecs;
     // texture slots (edxr_set_textures): descriptors and the texel pool with mip chains
     DevBuf tex_desc, tex_texels;
     uint32_t num_textures = 0;
@@ -443,6 +443,11 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     EDXR_CUDA(r->keybuf.ensure_zeroed(8 * samples * std::max<uint64_t>(pixels, 1), r->stream));
     const uint64_t icap = item_capacity(tiles, r->bin_capacity);
     EDXR_CUDA(r->items.ensure(sizeof(uint2) * icap));
+    // a vertex stage when vertices are shared (on average by at least three
+    // triangle corners): each is projected once instead of per corner
+    const bool vertex_stage = tv > 0 && tv <= tt;
+    if (vertex_stage)
+        EDXR_CUDA(r->vrecs.ensure(sizeof(int4) * tv));
 
     EDXR_CUDA(cudaMemcpyAsync(r->frames.ptr, r->frames_host, sizeof(FrameDesc) * n, cudaMemcpyHostToDevice, r->stream));
 
@@ -452,6 +457,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.frames = r->frames.as<FrameDesc>();
     a.num_frames = n;
     a.total_vertices = (uint32_t)tv;
+    a.vrecs = vertex_stage ? r->vrecs.as<int4>() : nullptr;
     a.total_tris = (uint32_t)tt;
     a.total_tiles = (uint32_t)tiles;
     a.rtris = r->rtris.as<RTri>();
@@ -652,7 +658,7 @@ edxr_status edxr_destroy(edxr_renderer* r)
     DevBuf* bufs[] = { &r->frames, &r->rtris, &r->polys, &r->clip_list, &r->tile_count, &r->tile_offset,
                        &r->tile_cursor, &r->bins, &r->bin_tmp, &r->big_list, &r->counters, &r->status, &r->color,
                        &r->depth, &r->tri_id, &r->back8, &r->diff_scratch, &r->tri_first, &r->items,
-                       &r->keybuf, &r->tex_desc, &r->tex_texels };
+                       &r->keybuf, &r->tex_desc, &r->tex_texels, &r->vrecs };
     for (DevBuf* b : bufs)
         b->release();
     for (auto& s : r->stage)

@@ -169,26 +169,25 @@ __device__ __forceinline__ uint32_t corner_code(int B, int C)
     return rej | (acc << 2);
 }
 
-// RasterTriangle::Setup (RasterTriangle.h:27-153) for three clip-space
-// vertices, plus the post-pass of Renderer.cpp:139-147 (invW = 1/w,
-// z *= invW).  Returns false for back-facing or degenerate triangles.
-__device__ __forceinline__ bool setup_triangle(const FrameDesc& f, float4 c0, float4 c1, float4 c2, RTri& t)
+// Per-vertex part of the setup: projection (x, y, z) / w with the
+// correctly rounded 1 / w, the raster transform and the snap to the 1/16
+// subpixel grid.
+__device__ __forceinline__ void project_vertex(const FrameDesc& f, float4 c, int& vx, int& vy, float& z, float& iw)
 {
-    const float4 cs[3] = { c0, c1, c2 };
-    int vx[3], vy[3];
-    float zp[3], iw[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-    {
-        const float invW = __frcp_rn(cs[k].w);  // == 1.0f / w, correctly rounded
-        const float hx = fmul(cs[k].x, invW), hy = fmul(cs[k].y, invW), hz = fmul(cs[k].z, invW);
-        float rx, ry;
-        xform_point3(f.raster, hx, hy, hz, rx, ry);
-        vx[k] = snap16(rx);
-        vy[k] = snap16(ry);
-        zp[k] = hz;
-        iw[k] = invW;
-    }
+    const float invW = __frcp_rn(c.w);  // == 1.0f / w, correctly rounded
+    const float hx = fmul(c.x, invW), hy = fmul(c.y, invW), hz = fmul(c.z, invW);
+    float rx, ry;
+    xform_point3(f.raster, hx, hy, hz, rx, ry);
+    vx = snap16(rx);
+    vy = snap16(ry);
+    z = hz;
+    iw = invW;
+}
+
+// Per-triangle part of the setup from the three projected vertices: edge
+// coefficients, determinant (culls det <= 0), 1 / det and the corners.
+__device__ __forceinline__ bool setup_projected(const int* vx, const int* vy, const float* zp, const float* iw, RTri& t)
+{
     const int B0 = wsub(vy[0], vy[1]), C0 = wsub(vx[1], vx[0]);
     const int B1 = wsub(vy[1], vy[2]), C1 = wsub(vx[2], vx[1]);
     const int B2 = wsub(vy[2], vy[0]), C2 = wsub(vx[0], vx[2]);
@@ -203,6 +202,19 @@ __device__ __forceinline__ bool setup_triangle(const FrameDesc& f, float4 c0, fl
     t.invW0 = iw[0]; t.invW1 = iw[1]; t.invW2 = iw[2];
     t.meta = corner_code(B0, C0) | (corner_code(B1, C1) << 4) | (corner_code(B2, C2) << 8);
     return true;
+}
+
+// RasterTriangle::Setup (RasterTriangle.h:27-153) for three clip-space
+// vertices, plus the post-pass of Renderer.cpp:139-147 (invW = 1/w,
+// z *= invW).  Returns false for back-facing or degenerate triangles.
+__device__ __forceinline__ bool setup_triangle(const FrameDesc& f, float4 c0, float4 c1, float4 c2, RTri& t)
+{
+    int vx[3], vy[3];
+    float zp[3], iw[3];
+    project_vertex(f, c0, vx[0], vy[0], zp[0], iw[0]);
+    project_vertex(f, c1, vx[1], vy[1], zp[1], iw[1]);
+    project_vertex(f, c2, vx[2], vy[2], zp[2], iw[2]);
+    return setup_projected(vx, vy, zp, iw, t);
 }
 
 // Edge coefficients B, C of a setup triangle (RasterTriangle.h:42-47).

@@ -136,6 +136,7 @@ struct PassArgs
     const FrameDesc* frames;
     uint32_t num_frames;
     uint32_t total_vertices;
+    int4* vrecs;             // per flattened vertex: setup record (vertex stage), or NULL: setup projects in place
     uint32_t total_tris;
     uint32_t total_tiles;
     RTri* rtris;             // slot i < total_tris: unclipped input triangle i; then fan pieces (counters[0])

@@ -24,10 +24,44 @@ constexpr uint32_t kBigChunk = 128;    // unsorted-list slots a k_bin_big warp r
 constexpr uint32_t kEmptySlot = 0xFFFFFFFFu;
 constexpr uint32_t kHeavyItem = 64;    // raster items with this many entries are handed out first
 
+// Clip-space position of vertex v: clip = MVP * (p, 1) (DefaultVertexShader,
+// Shader.h:40-49).
+__device__ __forceinline__ float4 clip_position(const FrameDesc& f, uint32_t v)
+{
+    const float* p = reinterpret_cast<const float*>(f.positions + (size_t)v * f.pos_stride);
+    return xform_point4(f.mvp, __ldg(p), __ldg(p + 1), __ldg(p + 2));
+}
+
+// Setup record of a vertex (vertex stage, for meshes whose vertices are
+// shared by several triangles): inside the view volume (clip code 0) the
+// projected vertex (x, y on the subpixel grid, z / w, 1 / w); otherwise
+// (kVtxOutside, clip code).
+constexpr int kVtxOutside = (int)0x80000000;
+
+__device__ __forceinline__ int4 vertex_record(const FrameDesc& f, uint32_t v)
+{
+    const float4 c = clip_position(f, v);
+    const uint32_t code = clip_code(c);
+    if (code)
+        return make_int4(kVtxOutside, (int)code, 0, 0);
+    int vx, vy;
+    float z, iw;
+    project_vertex(f, c, vx, vy, z, iw);
+    return make_int4(vx, vy, __float_as_int(z), __float_as_int(iw));
+}
+
 // -------------------------------------------------------------------------
+// Clear of the per-tile counters and work queues, and the vertex stage.
 __global__ void k_clear(PassArgs a)
 {
     const uint32_t stride = gridDim.x * blockDim.x;
+    if (a.vrecs)
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.total_vertices; i += stride)
+        {
+            const uint32_t fi = find_frame(a.frames, a.num_frames, i, [](const FrameDesc& f) { return f.vtx_base; });
+            const FrameDesc& f = a.frames[fi];
+            a.vrecs[i] = vertex_record(f, i - f.vtx_base);
+        }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= a.total_tiles; i += stride)
     {
         a.tile_count[i] = 0;
@@ -130,13 +164,6 @@ __device__ __forceinline__ void bin_big_append(const PassArgs& a, uint32_t ri, b
         a.big_list[b] = ri;
 }
 
-// Clip-space position of vertex v: clip = MVP * (p, 1) (DefaultVertexShader,
-// Shader.h:40-49), made where it is used instead of in a pass of its own.
-__device__ __forceinline__ float4 clip_position(const FrameDesc& f, uint32_t v)
-{
-    const float* p = reinterpret_cast<const float*>(f.positions + (size_t)v * f.pos_stride);
-    return xform_point4(f.mvp, __ldg(p), __ldg(p + 1), __ldg(p + 2));
-}
 
 // Appends n raster triangles for this lane with one atomic per warp; returns
 // the lane's first slot.  Every lane of the warp must call it.
@@ -191,23 +218,41 @@ __global__ void __launch_bounds__(256) k_setup(PassArgs a)
         }
         else
         {
-            const float4 c0 = clip_position(f, i0);
-            const float4 c1 = clip_position(f, i1);
-            const float4 c2 = clip_position(f, i2);
-            const uint32_t k0 = clip_code(c0), k1 = clip_code(c1), k2 = clip_code(c2);
-            if ((k0 | k1 | k2) == 0)
+            uint32_t k0, k1, k2;
+            if (a.vrecs)
             {
-                nOut = setup_triangle(f, c0, c1, c2, t) ? 1 : 0;
-                if (nOut)
+                // projected by the vertex stage
+                const int4 r0 = a.vrecs[f.vtx_base + i0], r1 = a.vrecs[f.vtx_base + i1], r2 = a.vrecs[f.vtx_base + i2];
+                k0 = r0.x == kVtxOutside ? (uint32_t)r0.y : 0u;
+                k1 = r1.x == kVtxOutside ? (uint32_t)r1.y : 0u;
+                k2 = r2.x == kVtxOutside ? (uint32_t)r2.y : 0u;
+                if ((k0 | k1 | k2) == 0)
                 {
-                    const BinGeom g = bin_geom(t, f);
-                    big = !g.small;
-                    if (g.small)
-                        nent = small_tiles(a, f, t, g, st);
+                    const int vx[3] = { r0.x, r1.x, r2.x }, vy[3] = { r0.y, r1.y, r2.y };
+                    const float zp[3] = { __int_as_float(r0.z), __int_as_float(r1.z), __int_as_float(r2.z) };
+                    const float iw[3] = { __int_as_float(r0.w), __int_as_float(r1.w), __int_as_float(r2.w) };
+                    nOut = setup_projected(vx, vy, zp, iw, t) ? 1 : 0;
                 }
             }
             else
-                straddle = !(k0 & k1 & k2);
+            {
+                const float4 c0 = clip_position(f, i0);
+                const float4 c1 = clip_position(f, i1);
+                const float4 c2 = clip_position(f, i2);
+                k0 = clip_code(c0);
+                k1 = clip_code(c1);
+                k2 = clip_code(c2);
+                if ((k0 | k1 | k2) == 0)
+                    nOut = setup_triangle(f, c0, c1, c2, t) ? 1 : 0;
+            }
+            if (nOut)
+            {
+                const BinGeom g = bin_geom(t, f);
+                big = !g.small;
+                if (g.small)
+                    nent = small_tiles(a, f, t, g, st);
+            }
+            straddle = (k0 | k1 | k2) != 0 && !(k0 & k1 & k2);
         }
     }
     // block-wide exclusive scans of (raster triangles, queued triangles),
@@ -1775,7 +1820,8 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
         if (ev) cudaEventRecord(ev[i], s);
     };
     mark(0);
-    k_clear<<<(a.total_tiles + 1 + 255) / 256 + 1, 256, 0, s>>>(a);
+    const uint32_t clear_items = max(a.total_tiles + 1, a.vrecs ? a.total_vertices : 0u);
+    k_clear<<<(clear_items + 255) / 256 + 1, 256, 0, s>>>(a);
     mark(1);
     if (a.total_tris)
     {
