@@ -27,7 +27,7 @@ constexpr uint32_t kNoTriangle = 0xFFFFFFFFu;
 constexpr uint32_t kItemEntries = 256;
 // Tile-count scan: tiles per block, and blocks (one status word each) of a pass.
 constexpr int kScanItems = 4;
-constexpr int kScanThreads = 1024;
+constexpr int kScanThreads = 256;
 constexpr int kScanBlock = kScanItems * kScanThreads;
 __host__ __device__ constexpr uint32_t scan_blocks(uint64_t tiles)
 {

@@ -871,7 +871,7 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* warp_sums, 
     __syncthreads();
     if (warp == 0)
     {
-        const uint32_t w = warp_sums[lane];
+        const uint32_t w = lane < (blockDim.x >> 5) ? warp_sums[lane] : 0u;
         uint32_t wi = w;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1)
