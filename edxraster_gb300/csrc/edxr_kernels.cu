@@ -700,7 +700,7 @@ __global__ void __launch_bounds__(kClipThreads) k_clip(PassArgs a)
 }
 
 // Scatter of the unsorted entries into their bins (after the scan); empty
-// slots are skipped.  Lanes with equal tiles share one atomic.
+// slots are skipped.
 __global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
 {
     const uint32_t n = *(volatile uint32_t*)&a.counters[5];
@@ -712,14 +712,36 @@ __global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
     {
         const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
         const uint2 e = i < m ? a.bin_tmp[i] : make_uint2(kEmptySlot, 0u);
-        const uint32_t peers = __match_any_sync(0xffffffffu, e.x);
+        uint32_t base = 0;
+        if (a.vrecs)
+        {
+            // a mesh with shared vertices: neighbouring lanes hold entries of
+            // neighbouring triangles, interleaved over the same few tiles;
+            // all lanes with equal tiles share one atomic
+            const uint32_t peers = __match_any_sync(0xffffffffu, e.x);
+            const int leader = __ffs(peers) - 1;
+            if ((int)lane == leader && e.x != kEmptySlot)
+                base = atomicAdd(&a.tile_cursor[e.x], (uint32_t)__popc(peers));
+            base = __shfl_sync(0xffffffffu, base, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+        }
+        else
+        {
+            // a triangle soup: lanes rarely share a tile, except in runs of
+            // consecutive lanes, which share one atomic
+            const uint32_t prev = __shfl_up_sync(0xffffffffu, e.x, 1);
+            const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0 || e.x != prev);
+            const uint32_t upto = 0xffffffffu >> (31 - lane);  // lanes 0..lane
+            const uint32_t head = 31 - __clz(heads & upto);
+            if (lane == head && e.x != kEmptySlot)
+            {
+                const uint32_t later = heads & ~upto;
+                const uint32_t end = later ? (uint32_t)__ffs(later) - 1u : 32u;
+                base = atomicAdd(&a.tile_cursor[e.x], end - lane);
+            }
+            base = __shfl_sync(0xffffffffu, base, head) + (lane - head);
+        }
         if (e.x == kEmptySlot)
             continue;
-        const int leader = __ffs(peers) - 1;
-        uint32_t base = 0;
-        if ((int)lane == leader)
-            base = atomicAdd(&a.tile_cursor[e.x], (uint32_t)__popc(peers));
-        base = __shfl_sync(peers, base, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
         const uint64_t pos = (uint64_t)a.tile_offset[e.x] + base;
         if (pos < a.bin_capacity)
             a.bins[pos] = e.y;
