@@ -24,7 +24,7 @@ constexpr uint32_t kNoTriangle = 0xFFFFFFFFu;
 // Raster work item: up to this many bin entries of one tile.  A tile with
 // more entries is split into several items whose winners are merged in a
 // per-pixel key buffer before the last of them shades the tile.
-constexpr uint32_t kItemEntries = 256;
+constexpr uint32_t kItemEntries = 128;
 // Tile-count scan: tiles per block, and blocks (one status word each) of a pass.
 constexpr int kScanItems = 4;
 constexpr int kScanThreads = 256;

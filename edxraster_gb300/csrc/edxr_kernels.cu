@@ -191,7 +191,7 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, int n)
 // the clip queue and the unsorted bin list are appended to with one atomic
 // per block each: the counters are single addresses every block of the grid
 // contends for.
-__global__ void __launch_bounds__(256) k_setup(PassArgs a)
+__global__ void __launch_bounds__(256, 6) k_setup(PassArgs a)
 {
     __shared__ uint32_t s_warp[8], s_went[8];
     __shared__ uint32_t s_base[3];
@@ -962,7 +962,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
     __syncthreads();
     const uint32_t prefix = s_prefix;
 
-    // offsets, and the items of this thread's tiles
+    // offsets, and the items of this thread's tiles.  A frame whose entries
+    // did not all fit (the unsorted list or the bins overflowed) is rendered
+    // again by the host; its tiles are made empty here, so no raster item
+    // reads a bin with missing entries or leaves a split tile's keys behind.
+    const bool dropped = *(volatile uint32_t*)&a.counters[5] > a.bin_capacity;
     uint32_t run = prefix + incl - sum;
     uint32_t nheavy = 0, nlight = 0;
     uint32_t start[kScanItems], n[kScanItems];
@@ -976,8 +980,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
         {
             a.tile_offset[i] = run;
             uint32_t c = cnt[k];
-            if ((uint64_t)run + c > a.bin_capacity)
-                c = 0;  // overflowed frame: k_raster skips the tile's entries too
+            if (dropped || (uint64_t)run + c > a.bin_capacity)
+            {
+                c = 0;
+                a.tile_count[i] = 0;
+            }
             n[k] = max(1u, (c + kItemEntries - 1) / kItemEntries);
             // only the last item of a tile can be light
             const uint32_t light = (c - (n[k] - 1) * kItemEntries) < kHeavyItem ? 1u : 0u;

@@ -64,6 +64,18 @@ def test_overflow_recovery_with_clipping(cuda_lib, monkeypatch):
     assert st.rerenders >= 1
 
 
+@pytest.mark.parametrize("seed", [31, 32, 33])
+def test_overflow_recovery_dense_tiles(cuda_lib, monkeypatch, seed):
+    """Tiny capacities on a scene with over 256 entries per tile (tiles
+    rasterized as several work items): the passes that overflow drop bin
+    entries and triangles, and must leave nothing behind (no bin read with
+    missing entries, no partial merge state) for the pass that renders the
+    frame in full."""
+    monkeypatch.setenv("EDXR_DEBUG_CAPACITY", "8")
+    st = assert_parity(scenes.small_random_scene(seed, 128, 96, ntris=1600))
+    assert st.rerenders >= 1
+
+
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_int32_wraparound_at_4k(cuda_lib, seed):
     """Screen-sized triangles at 3840x2160: edge functions of the coarse and
