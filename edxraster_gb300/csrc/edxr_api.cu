@@ -444,8 +444,10 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     const uint64_t icap = item_capacity(tiles, r->bin_capacity);
     EDXR_CUDA(r->items.ensure(sizeof(uint2) * icap));
     // a vertex stage when vertices are shared (on average by at least three
-    // triangle corners): each is projected once instead of per corner
-    const bool vertex_stage = tv > 0 && tv <= tt;
+    // triangle corners) and their records stay in L2 for setup to gather
+    // (up to 4 Mi vertices = 64 MiB of the 126 MiB): each vertex is then
+    // projected once instead of per corner
+    const bool vertex_stage = tv > 0 && tv <= tt && tv <= (4u << 20);
     if (vertex_stage)
         EDXR_CUDA(r->vrecs.ensure(sizeof(int4) * tv));
 
