@@ -1149,7 +1149,12 @@ __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uin
         for (int k = 0; k < 3; k++)
             G[k] = wadd(e.B[k], e.C[k]);
     }
-    const bool wf = !MS && wrap_free(t);
+    // wrap-free: covered pixel centres lie in the vertices' bounding box (the
+    // tight region, single sample only: an off-centre sample can be covered
+    // where the centre is not), and the depth bound below holds at every
+    // covered sample
+    const bool wfree = wrap_free(t);
+    const bool wf = !MS && wfree;
     int lx0 = 0, lx1 = 15, ly0 = 0, ly1 = 15;
     if (!accept)
     {
@@ -1173,7 +1178,7 @@ __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uin
     // submission order within the frame, offset by the frame's first input
     // triangle, so the winner's record is found from the rank alone
     s.rank = rank_base + t.order + 1u;
-    zkey = zmin_key(t, wf);
+    zkey = zmin_key(t, wfree);
 }
 
 // Key of the fragment of staged triangle s at tile pixel (lx, ly), or false
@@ -1592,15 +1597,22 @@ static __device__ __noinline__ void write_pixel_ms(const PassArgs& a, const Fram
 }
 
 // Raster with S samples per pixel: persistent warps on the same work items
-// as k_raster, keys [sample][pixel] in dynamic shared memory, every entry
-// rasterized pixel-parallel with a loop over the samples.  Split tiles merge
-// per sample in the key buffer (S planes).
+// as k_raster, keys [sample][pixel] in dynamic shared memory, every entry's
+// (entry, pixel) pairs spread over the lanes with a loop over the samples,
+// entries behind the tile's samples skipped.  Split tiles merge per sample
+// in the key buffer (S planes).
 constexpr int kMsRegionCap = 256;
 
 template <int S>
 __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
 {
     extern __shared__ unsigned long long ms_shared[];
+    // ceil(65536 / w): ((p * s_recip[w]) >> 16) == p / w for 0 <= p < 256
+    // and 1 <= w <= 16, the row of pixel p of a region w pixels wide
+    __shared__ uint32_t s_recip[17];
+    if (threadIdx.x >= 1 && threadIdx.x <= 16)
+        s_recip[threadIdx.x] = (65536u + threadIdx.x - 1u) / threadIdx.x;
+    __syncthreads();
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long* key = ms_shared + (size_t)warp * (256 * S + 32 * 10);
     StagedTri* staged = reinterpret_cast<StagedTri*>(key + 256 * S);            // 32 x 64 bytes
@@ -1638,10 +1650,11 @@ __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
             key[k] = clear;
         __syncwarp();
 
+        uint32_t tzmax = 0xBF800000u;  // largest depth key over the tile's samples so far
         for (uint32_t c = e0; c < e1; c += 32)
         {
             const uint32_t m = min(32u, e1 - c);
-            bool live = false;
+            int area = 0;
             if (lane < m)
             {
                 StagedTri st;
@@ -1649,37 +1662,66 @@ __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
                 int G[3];
                 stage_tri<true>(a, a.bins[c + lane], nr, f.tri_base << 4, tileX, tileY, st, zk, G);
                 const uint32_t fl = st.flags;
-                live = (fl & 31) <= ((fl >> 5) & 31) && ((fl >> 10) & 31) <= ((fl >> 15) & 31);
-                staged[lane] = st;
-                sg[3 * lane] = G[0];
-                sg[3 * lane + 1] = G[1];
-                sg[3 * lane + 2] = G[2];
-            }
-            uint32_t todo = __ballot_sync(0xffffffffu, live);
-            __syncwarp();
-            while (todo)
-            {
-                const int j = __ffs(todo) - 1;
-                todo &= todo - 1u;
-                const StagedTri st = staged[j];
-                const int G[3] = { sg[3 * j], sg[3 * j + 1], sg[3 * j + 2] };
-                const uint32_t fl = st.flags;
                 const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31, ry1 = (fl >> 15) & 31;
-                const int rw = rx1 - rx0 + 1, area = rw * (ry1 - ry0 + 1);
-                for (int p = (int)lane; p < area; p += 32)
+                if (zk <= tzmax && rx0 <= rx1 && ry0 <= ry1)
                 {
-                    const int dy = p / rw;
-                    const int x = rx0 + p - dy * rw, y = ry0 + dy;
+                    staged[lane] = st;
+                    sg[3 * lane] = G[0];
+                    sg[3 * lane + 1] = G[1];
+                    sg[3 * lane + 2] = G[2];
+                    area = (rx1 - rx0 + 1) * (ry1 - ry0 + 1);
+                }
+            }
+            // (entry, pixel) pairs numbered across the warp and taken 32 at a
+            // time, each lane testing the S samples of its pixel, so lanes do
+            // not idle on entries of a few pixels
+            int incl = area;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (uint32_t)o) incl += v;
+            }
+            const int pairs = __shfl_sync(0xffffffffu, incl, 31);
+            __syncwarp();
+            for (int base = 0; base < pairs; base += 32)
+            {
+                const int p = base + (int)lane;
+                // owner: the first lane whose inclusive count exceeds p
+                int j = 0;
+#pragma unroll
+                for (int st = 16; st >= 1; st >>= 1)
+                {
+                    const int v = __shfl_sync(0xffffffffu, incl, j + st - 1);
+                    if (v <= p) j += st;
+                }
+                const int first = __shfl_sync(0xffffffffu, incl - area, j);
+                if (p < pairs)
+                {
+                    const StagedTri st = staged[j];
+                    const int G[3] = { sg[3 * j], sg[3 * j + 1], sg[3 * j + 2] };
+                    const uint32_t fl = st.flags;
+                    const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31;
+                    const int rw = rx1 - rx0 + 1, local = p - first;
+                    const int dy = (int)(((uint32_t)local * s_recip[rw]) >> 16);
+                    const int x = rx0 + local - dy * rw, y = ry0 + dy;
 #pragma unroll 4
                     for (int s = 0; s < S; s++)
                     {
                         uint64_t k;
-                        unsigned long long& slot = key[s * 256 + y * 16 + x];
-                        if (sample_key(st, G, x, y, sample_offset(level, s), less, k) && k < slot)
-                            slot = k;
+                        unsigned long long* slot = &key[s * 256 + y * 16 + x];
+                        if (sample_key(st, G, x, y, sample_offset(level, s), less, k) && k < *slot)
+                            atomicMin(slot, (unsigned long long)k);
                     }
                 }
-                __syncwarp();
+            }
+            __syncwarp();
+            if (c + 32 < e1)
+            {
+                uint32_t mz = 0;
+                for (int k = (int)lane; k < 256 * S; k += 32)
+                    mz = max(mz, (uint32_t)(key[k] >> 32));
+                tzmax = __reduce_max_sync(0xffffffffu, mz);
             }
         }
 
