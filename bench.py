@@ -54,7 +54,7 @@ WORKLOADS = {
                lambda: scenes.stress_scene(1_000_000, 3840, 2160, seed=7)),
 }
 PIXEL_BYTES = 24  # RGBA32F colour + D32F depth + u32 triangle id per pixel
-E2E_RENDERERS = 3  # frames in flight in the end-to-end measurement
+E2E_RENDERERS = 4  # frames in flight in the end-to-end measurement
 
 
 def mesh_bytes(mesh) -> int:
@@ -396,10 +396,11 @@ def measure_diff(device, steps, warmup):
 def measure_e2e(sc, device, steps, warmup, workload, world=1, renderers=E2E_RENDERERS):
     """End to end through the public interface, as the reference's viewer
     drives it: every frame is RenderMesh on a mesh in pinned host memory
-    (uploaded by the call) followed by GetBackBuffer (the RGBA8 image read
+    (positions and indices uploaded by the call, normals and albedo read in
+    place by the shading) followed by GetBackBuffer (the RGBA8 image read
     back to the host).  `renderers` renderers, each with its own stream and
     host thread, keep frames in flight so uploads, kernels and read-backs of
-    different frames overlap; every frame still makes all of its own copies."""
+    different frames overlap; every frame still reads all of its own input."""
     import threading
     import torch
     from edxraster_gb300 import renderer as R
@@ -443,6 +444,9 @@ def measure_e2e(sc, device, steps, warmup, workload, world=1, renderers=E2E_REND
         r.close()
     return {"value": world * sc.mesh.nt * steps / elapsed / 1e6, "unit": "Mtris/s",
             "h2d_bytes_per_step": hmesh.nbytes(), "d2h_bytes_per_step": W * H * 4,
+            "h2d_copied_bytes_per_step": hmesh.copied_nbytes(),
+            "h2d_read_in_place": "normals and albedo (pinned) are read by the shading over NVLink-C2C: "
+                                 "only the winning triangles' vertex lines cross the link",
             "ms_per_step": elapsed * 1e3 / steps, "renderers_in_flight": renderers,
             "step": "RenderMesh(pinned host mesh) + GetBackBuffer (RGBA8 to host)"}
 

@@ -264,9 +264,28 @@ edxr_status check_mesh(const edxr_mesh* m)
     return EDXR_OK;
 }
 
+// Device address of host memory the GPU reads in place (page-locked memory
+// mapped into the device's address space, reached over NVLink-C2C), or NULL.
+const void* device_view(const void* p)
+{
+    if (!p)
+        return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 // Copy a host mesh to device staging buffers; returns a device-memory mesh.
-// Texture coordinates and texture ids are uploaded only for the textured
-// shader, the one that samples them.
+// Positions and indices, which the vertex stage, setup and clipping read
+// whole, are copied.  The shading-only arrays (normals, albedo; texture
+// coordinates and texture ids for the textured shader, the one that samples
+// them) are read in place when they are page-locked: only the lines of the
+// winning triangles' vertices then cross the host link.  Either way the
+// caller keeps the arrays unchanged until the frame completes.
 edxr_status stage_mesh(edxr_renderer* r, size_t slot, const edxr_mesh* in, edxr_mesh* out, bool textured = false)
 {
     *out = *in;
@@ -279,6 +298,15 @@ edxr_status stage_mesh(edxr_renderer* r, size_t slot, const edxr_mesh* in, edxr_
     auto copy = [&](DevBuf& buf, const void* src, uint32_t stride, size_t elem, const void** dst, uint32_t* dst_stride) -> edxr_status {
         if (!src)
             return EDXR_OK;
+        if (&buf != &s.pos)
+        {
+            if (const void* view = device_view(src))
+            {
+                *dst = view;
+                *dst_stride = stride;
+                return EDXR_OK;
+            }
+        }
         EDXR_CUDA(buf.ensure(nv * stride > 0 ? nv * stride : 16));
         if (nv)
             EDXR_CUDA(cudaMemcpyAsync(buf.ptr, src, (nv - 1) * (size_t)stride + elem, cudaMemcpyHostToDevice, r->stream));
@@ -293,7 +321,9 @@ edxr_status stage_mesh(edxr_renderer* r, size_t slot, const edxr_mesh* in, edxr_
     if (textured)
     {
         if ((st = copy(s.uv, in->uvs, in->uv_stride, 8, &out->uvs, &out->uv_stride))) return st;
-        if (in->texture_ids)
+        if (const void* view = device_view(in->texture_ids))
+            out->texture_ids = static_cast<const uint32_t*>(view);
+        else if (in->texture_ids)
         {
             const size_t tb = 4ull * in->num_triangles;
             EDXR_CUDA(s.tid.ensure(tb > 0 ? tb : 16));

@@ -81,10 +81,14 @@ class DeviceMesh:
 
 
 class HostMesh:
-    """A mesh in host memory (numpy), copied to the device by every render call."""
+    """A mesh in host memory (numpy) read by every render call: positions and
+    indices are copied to the device; with pinned=True (page-locked arrays)
+    the shading reads normals and albedo in place, otherwise they are copied
+    as well."""
 
     def __init__(self, mesh, pinned=False):
         self._keep = []
+        self.pinned = pinned
 
         def prep(a, dtype):
             a = np.ascontiguousarray(a, dtype)
@@ -105,9 +109,15 @@ class HostMesh:
         self.nv, self.nt = int(self.positions.shape[0]), int(self.indices.shape[0])
 
     def nbytes(self) -> int:
-        """Bytes one render call uploads (texture coordinates are not uploaded:
-        no shader samples them)."""
+        """Bytes of host input one render call reads (texture coordinates are
+        not read: no shader samples them)."""
         return sum(a.nbytes for a in (self.positions, self.normals, self.albedo, self.indices))
+
+    def copied_nbytes(self) -> int:
+        """Bytes one render call copies to the device: positions and indices,
+        plus normals and albedo unless they are pinned (read in place)."""
+        n = self.positions.nbytes + self.indices.nbytes
+        return n if self.pinned else n + self.normals.nbytes + self.albedo.nbytes
 
     def abi(self) -> _lib.Mesh:
         tid = None if self.texture_ids is None else self.texture_ids.ctypes.data

@@ -59,7 +59,7 @@ typedef struct edxr_renderer edxr_renderer;
 
 typedef enum edxr_memory
 {
-    EDXR_MEMORY_HOST = 0,   /* pointers are host memory; copied per call      */
+    EDXR_MEMORY_HOST = 0,   /* pointers are host memory, read per call (see edxr_mesh) */
     EDXR_MEMORY_DEVICE = 1  /* pointers are device memory of the renderer GPU */
 } edxr_memory;
 
@@ -147,7 +147,13 @@ typedef struct edxr_shader_params
  * are in bytes; positions, normals and albedo are three floats, uvs two.
  * The reference's interleaved Vertex_PositionNormalTex (32 bytes: position
  * at 0, normal at 12, uv at 24) is positions=base, normals=base+12,
- * uvs=base+24 with all strides 32. */
+ * uvs=base+24 with all strides 32.
+ * With EDXR_MEMORY_HOST, positions and indices are copied to the device by
+ * every render call; normals, albedo, uvs and texture ids are copied too,
+ * unless they are page-locked (cudaHostAlloc, cudaHostRegister): the
+ * shading then reads them in place, and only the winning triangles'
+ * vertices cross the host link.  Host arrays stay unchanged until the frame
+ * completes (edxr_synchronize). */
 typedef struct edxr_mesh
 {
     const void* positions; uint32_t position_stride;

@@ -142,6 +142,23 @@ def test_device_mesh_equals_host_mesh(cuda_lib):
     assert np.array_equal(c0, c1)
 
 
+def test_pinned_host_mesh_reads_attributes_in_place(cuda_lib):
+    """Page-locked normals and albedo are read in place by the shading; the
+    frame is identical to the one rendered from device memory."""
+    sc = scenes.small_random_scene(6, 128, 96, ntris=300)
+    outs = []
+    for mesh in (R.DeviceMesh.from_mesh(sc.mesh), R.HostMesh(sc.mesh, pinned=True), R.HostMesh(sc.mesh)):
+        r = R.Renderer()
+        r.Initialize(sc.view.width, sc.view.height)
+        R.configure(r, sc.view)
+        r.RenderMesh(mesh)
+        outs.append([a.copy() for a in r.ReadOutputs()])
+        r.close()
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
 def test_empty_mesh(cuda_lib):
     sc = scenes.small_random_scene(1, 40, 30, ntris=4)
     sc.mesh.indices = sc.mesh.indices[:0]

@@ -26,7 +26,8 @@ def render(sc, textures, texture_filter, msaa_log2=0, device_mesh=False):
     r.SetTextureFilter(texture_filter)
     if msaa_log2:
         r.SetMSAAMode(msaa_log2)
-    r.RenderMesh(R.DeviceMesh.from_mesh(sc.mesh) if device_mesh else sc.mesh)
+    r.RenderMesh(R.DeviceMesh.from_mesh(sc.mesh) if device_mesh == True else  # noqa: E712
+                 R.HostMesh(sc.mesh, pinned=True) if device_mesh == "pinned" else sc.mesh)
     out = r.ReadOutputs()
     r.close()
     return out
@@ -55,6 +56,8 @@ def test_textured_filters(cuda_lib, flt):
 def test_textured_device_mesh_and_msaa(cuda_lib):
     sc = scenes.textured_scene(160, 96, seed=1)
     check(sc, scenes.test_textures(1), R.FILTER_TRILINEAR, device_mesh=True)
+    # page-locked uvs and texture ids are read in place
+    check(sc, scenes.test_textures(1), R.FILTER_TRILINEAR, device_mesh="pinned")
     check(sc, scenes.test_textures(1), R.FILTER_LINEAR, msaa_log2=2)
 
 
