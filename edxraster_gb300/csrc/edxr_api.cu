@@ -157,7 +157,7 @@ struct edxr_renderer
     Shading shading;
     Camera cam;
 
-    DevBuf frames, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, bins, bin_tmp, big_list, counters,
+    DevBuf frames, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, tile_zocc, bins, bin_tmp, big_list, counters,
         status;
     DevBuf color, depth, tri_id, back8, diff_scratch, tri_first, items, keybuf, vrecs;
     // texture slots (edxr_set_textures): descriptors and the texel pool with mip chains
@@ -460,6 +460,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     EDXR_CUDA(r->tile_count.ensure(4 * (tiles + 1)));
     EDXR_CUDA(r->tile_offset.ensure(4 * (tiles + 1)));
     EDXR_CUDA(r->tile_cursor.ensure(4 * (tiles + 1)));
+    EDXR_CUDA(r->tile_zocc.ensure(4 * (tiles + 1)));
     EDXR_CUDA(r->bins.ensure(4 * r->bin_capacity));
     EDXR_CUDA(r->bin_tmp.ensure(8 * r->bin_capacity));
     EDXR_CUDA(r->big_list.ensure(4 * r->big_cap));
@@ -500,6 +501,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.tile_count = r->tile_count.as<uint32_t>();
     a.tile_offset = r->tile_offset.as<uint32_t>();
     a.tile_cursor = r->tile_cursor.as<uint32_t>();
+    a.tile_zocc = r->tile_zocc.as<uint32_t>();
     a.bins = r->bins.as<uint32_t>();
     a.bin_tmp = r->bin_tmp.as<uint2>();
     a.bin_capacity = r->bin_capacity;
@@ -688,7 +690,7 @@ edxr_status edxr_destroy(edxr_renderer* r)
     if (r->graph)
         cudaGraphExecDestroy(r->graph);
     DevBuf* bufs[] = { &r->frames, &r->rtris, &r->polys, &r->clip_list, &r->tile_count, &r->tile_offset,
-                       &r->tile_cursor, &r->bins, &r->bin_tmp, &r->big_list, &r->counters, &r->status, &r->color,
+                       &r->tile_cursor, &r->tile_zocc, &r->bins, &r->bin_tmp, &r->big_list, &r->counters, &r->status, &r->color,
                        &r->depth, &r->tri_id, &r->back8, &r->diff_scratch, &r->tri_first, &r->items,
                        &r->keybuf, &r->tex_desc, &r->tex_texels, &r->vrecs };
     for (DevBuf* b : bufs)

@@ -146,6 +146,8 @@ struct PassArgs
     uint32_t* clip_list;     // input triangles (flattened) that straddle a clip plane
     uint32_t* tile_count;    // total_tiles + 1
     uint32_t* tile_offset;   // total_tiles + 1 (exclusive scan of padded counts)
+    uint32_t* tile_zocc;     // total_tiles + 1; per tile the least far-depth key of the triangles accepted
+                             // over it whole (entries beyond it are hidden), ~0 for none
     uint32_t* tile_cursor;   // total_tiles + 1; the scatter's cursors, then entries of split tiles not yet rastered
     uint32_t* bins;
     uint2* bin_tmp;          // decided (tile, entry) pairs before the scatter, bin_capacity of them

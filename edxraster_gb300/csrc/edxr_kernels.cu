@@ -65,6 +65,7 @@ __global__ void k_clear(PassArgs a)
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= a.total_tiles; i += stride)
     {
         a.tile_count[i] = 0;
+        a.tile_zocc[i] = 0xFFFFFFFFu;
         a.tile_cursor[i] = 0;
     }
     if (blockIdx.x == 0 && threadIdx.x < kCounters)
@@ -748,6 +749,23 @@ __global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
     }
 }
 
+// Upper bound (as a depth key) of every depth the reference computes for
+// the triangle at a pixel of a 16x16 block it trivially accepts, or ~0 (no
+// bound) when its edge values can wrap or its depths are not finite.  The
+// block's corners are inside every edge, so are all its pixel centres: the
+// barycentrics are within a few ulps of [0, 1] and the depth at most max(z)
+// plus a few ulps of the |z| sum.  Every entry of the tile whose lower bound
+// lies beyond it loses at every pixel to this triangle's fragment.
+__device__ __forceinline__ uint32_t zmax_key(const RTri& t)
+{
+    if (!wrap_free(t))
+        return 0xFFFFFFFFu;
+    const float zmax = fmaxf(t.z0, fmaxf(t.z1, t.z2));
+    const float margin = 2e-6f * (fabsf(t.z0) + fabsf(t.z1) + fabsf(t.z2)) + 1e-30f;
+    const float hi = zmax + margin;
+    return (hi == hi && fabsf(hi) <= 3.0e38f && fabsf(t.invDet) <= 3.0e38f) ? depth_key(hi) : 0xFFFFFFFFu;
+}
+
 // Big triangles, up to 32 at a time per warp: their (triangle, 32x32 reference
 // tile) pairs are numbered across the warp and taken 32 at a time, each lane
 // deciding the four quadrants of its pair's tile, so a triangle with few
@@ -771,7 +789,7 @@ __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
     for (uint32_t b0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * batch; b0 < nb; b0 += nw * batch)
     {
         // this lane's triangle of the batch and its number of 32x32 tiles
-        uint32_t mine = kNoTriangle;
+        uint32_t mine = kNoTriangle, mine_zocc = 0xFFFFFFFFu;
         int n = 0;
         if (lane < batch && b0 + lane < nb)
         {
@@ -779,6 +797,7 @@ __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
             const RTri t = a.rtris[mine];
             const BinGeom g = bin_geom(t, a.frames[t.meta >> 12]);
             n = (g.t32x1 - g.t32x0 + 1) * (g.t32y1 - g.t32y0 + 1);
+            mine_zocc = zmax_key(t);
         }
         int incl = n;
 #pragma unroll
@@ -801,6 +820,9 @@ __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
             }
             const int first = __shfl_sync(0xffffffffu, incl - n, j);
             const uint32_t ri = __shfl_sync(0xffffffffu, mine, j);
+            // an accepted quadrant is covered whole: the triangle's far depth
+            // bounds the tile
+            const uint32_t zocc = __shfl_sync(0xffffffffu, mine_zocc, j);
             uint32_t dq = 0, tile00 = 0;
             int tdx = 0;
             if (p < pairs)
@@ -845,6 +867,8 @@ __global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
                     continue;
                 const uint32_t tile = tile00 + (uint32_t)((q >> 1) * tdx + (q & 1));
                 atomicAdd(&a.tile_count[tile], 1u);
+                if (d == kDecisionAccept && zocc != 0xFFFFFFFFu)
+                    atomicMin(&a.tile_zocc[tile], zocc);
                 if (pos < a.bin_capacity)
                     a.bin_tmp[pos] = make_uint2(tile, (ri << 2) | d);
                 pos++;
@@ -1322,7 +1346,10 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
         for (int k = 0; k < 8; k++)
             key[lane + 32 * k] = clear;
         __syncwarp();
-        uint32_t tzmax = 0xBF800000u;  // largest depth key of the tile's pixels so far
+        // depth bound of the tile: the nearest triangle that covers it whole,
+        // then the largest depth key of its pixels so far
+        const uint32_t tzocc = min(0xBF800000u, a.tile_zocc[tile]);
+        uint32_t tzmax = tzocc;
 
         for (uint32_t c = e0; c < e1; c += 32)
         {
@@ -1413,7 +1440,7 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
 #pragma unroll
                 for (int k = 0; k < 8; k++)
                     mz = max(mz, (uint32_t)(key[lane + 32 * k] >> 32));
-                tzmax = __reduce_max_sync(0xffffffffu, mz);
+                tzmax = min(tzocc, __reduce_max_sync(0xffffffffu, mz));
             }
         }
 
@@ -1650,7 +1677,10 @@ __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
             key[k] = clear;
         __syncwarp();
 
-        uint32_t tzmax = 0xBF800000u;  // largest depth key over the tile's samples so far
+        // depth bound of the tile: the nearest triangle that covers it whole
+        // (every sample), then the largest depth key of its samples so far
+        const uint32_t tzocc = min(0xBF800000u, a.tile_zocc[tile]);
+        uint32_t tzmax = tzocc;
         for (uint32_t c = e0; c < e1; c += 32)
         {
             const uint32_t m = min(32u, e1 - c);
@@ -1721,7 +1751,7 @@ __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
                 uint32_t mz = 0;
                 for (int k = (int)lane; k < 256 * S; k += 32)
                     mz = max(mz, (uint32_t)(key[k] >> 32));
-                tzmax = __reduce_max_sync(0xffffffffu, mz);
+                tzmax = min(tzocc, __reduce_max_sync(0xffffffffu, mz));
             }
         }
 

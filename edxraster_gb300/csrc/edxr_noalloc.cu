@@ -58,7 +58,8 @@ constexpr size_t kOffClipList = align256(kOffPoly + sizeof(ClipPoly) * (size_t)k
 constexpr size_t kOffCount = align256(kOffClipList + 4 * (size_t)kPolyCap);
 constexpr size_t kOffOffset = align256(kOffCount + 4 * (size_t)(kMaxTiles + 1));
 constexpr size_t kOffCursor = align256(kOffOffset + 4 * (size_t)(kMaxTiles + 1));
-constexpr size_t kOffBins = align256(kOffCursor + 4 * (size_t)(kMaxTiles + 1));
+constexpr size_t kOffZocc = align256(kOffCursor + 4 * (size_t)(kMaxTiles + 1));
+constexpr size_t kOffBins = align256(kOffZocc + 4 * (size_t)(kMaxTiles + 1));
 constexpr size_t kOffBinTmp = align256(kOffBins + 4 * (size_t)kBinCap);
 constexpr size_t kOffBig = align256(kOffBinTmp + 8 * (size_t)kBinCap);
 constexpr size_t kOffCounters = align256(kOffBig + 4 * (size_t)kBigCap);
@@ -256,6 +257,7 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
     a.tile_count = reinterpret_cast<uint32_t*>(base + kOffCount);
     a.tile_offset = reinterpret_cast<uint32_t*>(base + kOffOffset);
     a.tile_cursor = reinterpret_cast<uint32_t*>(base + kOffCursor);
+    a.tile_zocc = reinterpret_cast<uint32_t*>(base + kOffZocc);
     a.bins = reinterpret_cast<uint32_t*>(base + kOffBins);
     a.bin_tmp = reinterpret_cast<uint2*>(base + kOffBinTmp);
     a.bin_capacity = kBinCap;

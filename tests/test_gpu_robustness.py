@@ -76,6 +76,38 @@ def test_overflow_recovery_dense_tiles(cuda_lib, monkeypatch, seed):
     assert st.rerenders >= 1
 
 
+@pytest.mark.parametrize("depth_func", [R.DEPTH_LEQUAL, R.DEPTH_LESS])
+def test_occluders_cull_only_hidden_entries(cuda_lib, depth_func):
+    """Tiles covered whole by a triangle skip the entries beyond its far
+    depth.  Planes at equal and nearly equal depths (ties decided by
+    submission order), triangles that straddle the occluder's depth, small
+    ones in front of and just behind it: all winners as the oracle's."""
+    rng = np.random.default_rng(5)
+    tris = []
+    for k in range(300):
+        z = float(rng.choice([0.3, 0.3, 0.5, np.nextafter(np.float32(0.3), np.float32(1.0))]))
+        if k % 3 == 0:  # screen-covering quad halves (accepted over whole tiles)
+            quad = [(-1.2, -1.2), (1.2, -1.2), (1.2, 1.2), (-1.2, 1.2)]
+            t1 = [(x, y, z, 1.0) for x, y in (quad[0], quad[2], quad[1])]
+            t2 = [(x, y, z, 1.0) for x, y in (quad[0], quad[3], quad[2])]
+            tris += [t1, t2]
+        else:
+            c = rng.uniform(-0.9, 0.9, size=2)
+            xy = c + rng.uniform(-0.3, 0.3, size=(3, 2))
+            zs = z + rng.uniform(-0.05, 0.05, size=3) * (k % 2)
+            t = [(x, y, float(zz), 1.0) for (x, y), zz in zip(xy, zs)]
+            a = np.cross(np.r_[xy[1] - xy[0], 0], np.r_[xy[2] - xy[0], 0])[2]
+            if a > 0:  # clockwise on screen (raster y points down)
+                t = [t[0], t[2], t[1]]
+            tris.append(t)
+    sc = clip_space_scene(tris, 160, 128)
+    sc.view.depth_func = depth_func
+    (c, d, t), _ = gpu(sc)
+    o = pyoracle.render_oracle(sc.mesh, sc.view, depth_func=depth_func)
+    assert not mismatch_report("triangle id", t, o["id"])
+    assert not mismatch_report("depth", d.view(np.uint32), o["depth"].view(np.uint32))
+
+
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_int32_wraparound_at_4k(cuda_lib, seed):
     """Screen-sized triangles at 3840x2160: edge functions of the coarse and
