@@ -773,7 +773,7 @@ __device__ __forceinline__ uint32_t zmax_key(const RTri& t)
 // kept in the unsorted list, which the warp fills from slots it reserves
 // kBigChunk at a time (one atomic on the shared counter per chunk); slots
 // it leaves unused are marked empty.
-__global__ void __launch_bounds__(256) k_bin_big(PassArgs a)
+__global__ void __launch_bounds__(256, 4) k_bin_big(PassArgs a)
 {
     const uint32_t nb = min(*(volatile uint32_t*)&a.counters[2], a.big_capacity);
     const uint32_t lane = threadIdx.x & 31;
