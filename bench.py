@@ -148,6 +148,25 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """The largest x over all ranks: the job's time is its slowest rank's.
+    Every rank renders its own replica of the workload (frames are
+    independent; there is no exchange step), so this is the only collective."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world: int, units_per_rank: int, steps: int, total_ms: float) -> float:
+    """Whole-job throughput (millions of units per second) of `world` ranks
+    that each processed units_per_rank x steps units in at most total_ms."""
+    return world * units_per_rank * steps / (total_ms / 1e3) / 1e6
+
+
 def cpu_oracle_time(sc, threads: int):
     from oracle import pyoracle
     t0 = time.perf_counter()
@@ -435,14 +454,10 @@ def measure_e2e(sc, device, steps, warmup, workload, world=1, renderers=E2E_REND
     t0 = time.perf_counter()
     run(steps)
     torch.cuda.synchronize()
-    elapsed = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([elapsed], device="cuda:%d" % device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(time.perf_counter() - t0, world, "cuda:%d" % device)
     for r in rs:
         r.close()
-    return {"value": world * sc.mesh.nt * steps / elapsed / 1e6, "unit": "Mtris/s",
+    return {"value": job_throughput(world, sc.mesh.nt, steps, elapsed * 1e3), "unit": "Mtris/s",
             "h2d_bytes_per_step": hmesh.nbytes(), "d2h_bytes_per_step": W * H * 4,
             "h2d_copied_bytes_per_step": hmesh.copied_nbytes(),
             "h2d_read_in_place": "normals and albedo (pinned) are read by the shading over NVLink-C2C: "
@@ -495,15 +510,11 @@ def run_gpu(args, world, rank, local):
     torch.cuda.synchronize()
     clock_info = clocks.stop()
     per = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(per)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda:%d" % local)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(per), world, "cuda:%d" % local)
     stats = r.Stats()
     r_tuning = r.GetTuning()
     ms_per_step = total_ms / args.steps
-    value = world * sc.mesh.nt * args.steps / (total_ms / 1e3) / 1e6
+    value = job_throughput(world, sc.mesh.nt, args.steps, total_ms)
 
     # ---- stage times (dominant kernel) ---------------------------------
     r.SetProfiling(True)
