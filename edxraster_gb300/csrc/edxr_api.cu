@@ -473,7 +473,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     EDXR_CUDA(r->tri_id.ensure(4 * samples * std::max<uint64_t>(pixels, 1)));
     EDXR_CUDA(r->keybuf.ensure_zeroed(8 * samples * std::max<uint64_t>(pixels, 1), r->stream));
     const uint64_t icap = item_capacity(tiles, r->bin_capacity);
-    EDXR_CUDA(r->items.ensure(sizeof(uint2) * icap));
+    EDXR_CUDA(r->items.ensure(sizeof(uint4) * icap));
     // a vertex stage when vertices are shared (on average by at least three
     // triangle corners) and their records stay in L2 for setup to gather
     // (up to 4 Mi vertices = 64 MiB of the 126 MiB): each vertex is then
@@ -514,7 +514,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.depth = r->depth.as<float>();
     a.tri_id = r->tri_id.as<uint32_t>();
     a.tri_first = r->tri_first.as<uint32_t>();
-    a.items = r->items.as<uint2>();
+    a.items = r->items.as<uint4>();
     a.item_capacity = icap;
     a.keybuf = r->keybuf.as<unsigned long long>();
     a.total_pixels = pixels;
@@ -608,8 +608,8 @@ edxr_status sync_pass(edxr_renderer* r)
             a.bin_tmp = r->bin_tmp.as<uint2>();
             a.bin_capacity = r->bin_capacity;
             a.item_capacity = item_capacity(a.total_tiles, r->bin_capacity);
-            EDXR_CUDA(r->items.ensure(sizeof(uint2) * a.item_capacity));
-            a.items = r->items.as<uint2>();
+            EDXR_CUDA(r->items.ensure(sizeof(uint4) * a.item_capacity));
+            a.items = r->items.as<uint4>();
         }
         r->rerenders++;
         EDXR_CUDA(run_pass(r, a));

@@ -159,8 +159,8 @@ struct PassArgs
                              // [8] scan block tickets, [10] unclipped surviving triangles,
                              // [11] surviving fan pieces (kCounters words)
     unsigned long long* scan_status;  // per scan block (scan_blocks(total_tiles) words)
-    uint2* items;            // raster work items (tile, index of its kItemEntries-entry slice): heavy ones
-                             // from the front, light ones from the back
+    uint4* items;            // raster work items (tile | split flag, first entry, end entry, 0), one per
+                             // kItemEntries-entry slice: heavy ones from the front, light ones from the back
     uint64_t item_capacity;
     unsigned long long* keybuf;  // per pixel: ~(smallest key) of split tiles, 0 between passes
     DeviceStatus* status;

@@ -22,6 +22,7 @@ namespace edxr {
 constexpr int kRasterThreads = 256;    // 8 warps, each on its own work items
 constexpr uint32_t kBigChunk = 128;    // unsorted-list slots a k_bin_big warp reserves at a time
 constexpr uint32_t kEmptySlot = 0xFFFFFFFFu;
+constexpr uint32_t kSplitTile = 0x80000000u;  // item tag: the tile has several items (tiles < 2^24)
 constexpr uint32_t kHeavyItem = 64;    // raster items with this many entries are handed out first
 
 // Clip-space position of vertex v: clip = MVP * (p, 1) (DefaultVertexShader,
@@ -1048,13 +1049,16 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
             continue;
         const bool light = (cnt[k] - (n[k] - 1) * kItemEntries) < kHeavyItem;
         const uint32_t heavy = n[k] - (light ? 1u : 0u);
+        const uint32_t end = start[k] + cnt[k];
+        const uint32_t tag = i | (n[k] > 1 ? kSplitTile : 0u);
         for (uint32_t j = 0; j < heavy; j++, hbase++)
             if (hbase < a.item_capacity)
-                a.items[hbase] = make_uint2(i, j);
+                a.items[hbase] = make_uint4(tag, start[k] + j * kItemEntries,
+                                            min(end, start[k] + (j + 1) * kItemEntries), 0u);
         if (light)
         {
             if (lbase < a.item_capacity)
-                a.items[a.item_capacity - 1 - lbase] = make_uint2(i, n[k] - 1);
+                a.items[a.item_capacity - 1 - lbase] = make_uint4(tag, start[k] + (n[k] - 1) * kItemEntries, end, 0u);
             lbase++;
         }
     }
@@ -1242,6 +1246,17 @@ struct __align__(16) StagedSlot
     uint4 pad;
 };
 
+// The next work item of a persistent raster warp: after the first (item
+// number = the warp's index in the grid, no claim), items first_items,
+// first_items + 1, ... are claimed one at a time.
+__device__ __forceinline__ uint32_t claim_item(const PassArgs& a, uint32_t first_items)
+{
+    uint32_t q = 0;
+    if ((threadIdx.x & 31) == 0)
+        q = first_items + atomicAdd(&a.counters[3], 1u);
+    return __shfl_sync(0xffffffffu, q, 0);
+}
+
 // Raster triangle of the fragment with submission rank `rank` (0: none), or
 // kNoTriangle.  rank - 1 = flattened input triangle * 16 + fan field: 0 for a
 // triangle that was not clipped, whose record sits at its flattened index;
@@ -1318,27 +1333,20 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
     const uint32_t nitems = (uint32_t)min((uint64_t)nheavy + *(volatile uint32_t*)&a.counters[7], a.item_capacity);
     const int small_region = min(a.tune.small_region, 64);
     const PixelOut out = { a.rtris, a.polys, a.color, a.depth, a.tri_id };
-    for (;;)
+    // each warp's first item is its own (the heaviest ones, no claim), the
+    // rest are claimed one at a time
+    for (uint32_t q = blockIdx.x * kRasterWarps + warp; q < nitems; q = claim_item(a, gridDim.x * kRasterWarps))
     {
-        uint32_t q = 0;
-        if (lane == 0)
-            q = atomicAdd(&a.counters[3], 1u);
-        q = __shfl_sync(0xffffffffu, q, 0);
-        if (q >= nitems)
-            break;
-        const uint2 item = a.items[q < nheavy ? q : (uint32_t)(a.item_capacity - 1 - (q - nheavy))];
-        const uint32_t tile = item.x;
+        const uint4 item = a.items[q < nheavy ? q : (uint32_t)(a.item_capacity - 1 - (q - nheavy))];
+        const uint32_t tile = item.x & ~kSplitTile;
         const uint32_t fi = find_frame(a.frames, a.num_frames, tile, [](const FrameDesc& f) { return f.tile_base; });
         const FrameDesc& f = a.frames[fi];
         const uint32_t lt = tile - f.tile_base;
         const int tileX = (int)(lt % (uint32_t)f.tdx), tileY = (int)(lt / (uint32_t)f.tdx);
         const bool less = f.depth_func == 1;
-        uint32_t count = a.tile_count[tile];
-        const uint32_t start = a.tile_offset[tile];
-        if ((uint64_t)start + count > a.bin_capacity)
-            count = 0;  // overflowed frame: rendered again by the host
-        const uint32_t e0 = start + item.y * kItemEntries;
-        const uint32_t e1 = min(start + count, e0 + kItemEntries);
+        // (a frame whose entries overflowed has empty items: rendered again by the host)
+        const uint32_t e0 = item.y, e1 = item.z;
+        const bool split = (item.x & kSplitTile) != 0;
 
         // clear depth 1.0 with no triangle: rank term ~0 (LEQUAL) or 0 (LESS)
         const unsigned long long clear = ((unsigned long long)0xBF800000u << 32) | (less ? 0u : 0xFFFFFFFFu);
@@ -1448,7 +1456,7 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
         // the item that finishes last (the tile's cursor, equal to its entry
         // count after the scatter, counted down to zero) shades the tile.
         bool shade = true;
-        if (count > kItemEntries)
+        if (split)
         {
 #pragma unroll
             for (int k = 0; k < 8; k++)
@@ -1651,27 +1659,21 @@ __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
     const uint32_t nheavy = *(volatile uint32_t*)&a.counters[6];
     const uint32_t nitems = (uint32_t)min((uint64_t)nheavy + *(volatile uint32_t*)&a.counters[7], a.item_capacity);
     const uint64_t plane = a.total_pixels;
-    for (;;)
+    // each warp's first item is its own (the heaviest ones, no claim), the
+    // rest are claimed one at a time
+    for (uint32_t q = blockIdx.x * (blockDim.x >> 5) + warp; q < nitems;
+         q = claim_item(a, gridDim.x * (blockDim.x >> 5)))
     {
-        uint32_t q = 0;
-        if (lane == 0)
-            q = atomicAdd(&a.counters[3], 1u);
-        q = __shfl_sync(0xffffffffu, q, 0);
-        if (q >= nitems)
-            break;
-        const uint2 item = a.items[q < nheavy ? q : (uint32_t)(a.item_capacity - 1 - (q - nheavy))];
-        const uint32_t tile = item.x;
+        const uint4 item = a.items[q < nheavy ? q : (uint32_t)(a.item_capacity - 1 - (q - nheavy))];
+        const uint32_t tile = item.x & ~kSplitTile;
         const uint32_t fi = find_frame(a.frames, a.num_frames, tile, [](const FrameDesc& f) { return f.tile_base; });
         const FrameDesc& f = a.frames[fi];
         const uint32_t lt = tile - f.tile_base;
         const int tileX = (int)(lt % (uint32_t)f.tdx), tileY = (int)(lt / (uint32_t)f.tdx);
         const bool less = f.depth_func == 1;
-        uint32_t count = a.tile_count[tile];
-        const uint32_t start = a.tile_offset[tile];
-        if ((uint64_t)start + count > a.bin_capacity)
-            count = 0;  // overflowed frame: rendered again by the host
-        const uint32_t e0 = start + item.y * kItemEntries;
-        const uint32_t e1 = min(start + count, e0 + kItemEntries);
+        // (a frame whose entries overflowed has empty items: rendered again by the host)
+        const uint32_t e0 = item.y, e1 = item.z;
+        const bool split = (item.x & kSplitTile) != 0;
         const unsigned long long clear = ((unsigned long long)0xBF800000u << 32) | (less ? 0u : 0xFFFFFFFFu);
         for (int k = (int)lane; k < 256 * S; k += 32)
             key[k] = clear;
@@ -1756,7 +1758,7 @@ __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
         }
 
         bool shade = true;
-        if (count > kItemEntries)
+        if (split)
         {
             for (int k = (int)lane; k < 256 * S; k += 32)
             {

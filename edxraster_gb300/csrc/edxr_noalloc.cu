@@ -67,7 +67,7 @@ constexpr size_t kOffStatus = align256(kOffCounters + 4 * kCounters + 8 * (size_
 constexpr size_t kOffTriFirst = align256(kOffStatus + sizeof(DeviceStatus));
 constexpr size_t kItemCap = item_capacity(kMaxTiles, kBinCap);
 constexpr size_t kOffItems = align256(kOffTriFirst + 4 * (size_t)kMaxTriangles);
-constexpr size_t kOffKeyBuf = align256(kOffItems + sizeof(uint2) * kItemCap);
+constexpr size_t kOffKeyBuf = align256(kOffItems + sizeof(uint4) * kItemCap);
 constexpr size_t kNoAllocScratchBytes = align256(kOffKeyBuf + 8 * (size_t)kMaxPixels);
 
 // The scratch of edxr_render_noalloc (about 24 MiB per device).  Host code
@@ -270,7 +270,7 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
     a.depth = depth;
     a.tri_id = triangle_id;
     a.tri_first = reinterpret_cast<uint32_t*>(base + kOffTriFirst);
-    a.items = reinterpret_cast<uint2*>(base + kOffItems);
+    a.items = reinterpret_cast<uint4*>(base + kOffItems);
     a.item_capacity = kItemCap;
     // zero in the array's initial image, and every pass leaves it zero
     a.keybuf = reinterpret_cast<unsigned long long*>(base + kOffKeyBuf);
