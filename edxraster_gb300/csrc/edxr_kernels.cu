@@ -1359,16 +1359,21 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
         const uint32_t tzocc = min(0xBF800000u, a.tile_zocc[tile]);
         uint32_t tzmax = tzocc;
 
+        // each chunk's bin entries load while the previous chunk is rasterized
+        uint32_t next = e0 + lane < e1 ? a.bins[e0 + lane] : 0u;
         for (uint32_t c = e0; c < e1; c += 32)
         {
             const uint32_t m = min(32u, e1 - c);
+            const uint32_t entry = next;
+            if (c + 32 + lane < e1)
+                next = a.bins[c + 32 + lane];
             int nsmall = 0;
             bool big = false;
             if (lane < m)
             {
                 StagedTri s;
                 uint32_t zk;
-                stage_tri(a, a.bins[c + lane], nr, f.tri_base << 4, tileX, tileY, s, zk);
+                stage_tri(a, entry, nr, f.tri_base << 4, tileX, tileY, s, zk);
                 const uint32_t fl = s.flags;
                 const int rx0 = fl & 31, rx1 = (fl >> 5) & 31, ry0 = (fl >> 10) & 31, ry1 = (fl >> 15) & 31;
                 if (zk <= tzmax && rx0 <= rx1 && ry0 <= ry1)
