@@ -154,7 +154,7 @@ struct PassArgs
     uint64_t bin_capacity;
     uint32_t* big_list;      // raster triangles with many tiles, binned by whole blocks
     uint32_t big_capacity;
-    uint32_t* counters;      // [0] fan-piece slots, [1] polys, [2] big tris, [3] raster work queue, [4] clip list,
+    uint32_t* counters;      // [0] fan-piece slots, [2] big tris, [3] raster work queue, [4] clip list,
                              // [5] unsorted bin list slots, [6] heavy raster work items, [7] light ones,
                              // [8] scan block tickets, [10] unclipped surviving triangles,
                              // [11] surviving fan pieces (kCounters words)

@@ -1076,9 +1076,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
         a.status->big_tris = a.counters[2];
         if ((uint64_t)a.total_tris + a.counters[0] > a.rtri_capacity)
             atomicOr(&a.status->overflow, 2u);
-        if (a.counters[1] > a.poly_capacity || a.counters[4] > a.poly_capacity)
+        if (a.counters[4] > a.poly_capacity)
             atomicOr(&a.status->overflow, 4u);
-        a.status->clipped_polys = max(a.counters[1], a.counters[4]);
+        a.status->clipped_polys = a.counters[4];  // one polygon record per queued triangle
         if (needed > a.bin_capacity)
             atomicOr(&a.status->overflow, 1u);
         if (a.counters[2] > a.big_capacity)
