@@ -1641,7 +1641,6 @@ static __device__ __noinline__ void write_pixel_ms(const PassArgs& a, const Fram
 // (entry, pixel) pairs spread over the lanes with a loop over the samples,
 // entries behind the tile's samples skipped.  Split tiles merge per sample
 // in the key buffer (S planes).
-constexpr int kMsRegionCap = 256;
 
 template <int S>
 __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
