@@ -375,9 +375,10 @@ def measure_diff(device, steps, warmup):
                        g_glob.data_ptr() + 12, g_glob.data_ptr() + 16)
     abi = dm.abi()
     loss = torch.zeros((), device=dev)
+    batch = r.PrepareBatch([dm], views)  # the views' ABI records, built once
 
     def forward():
-        r.RenderBatched([dm], views, 256, 256, synchronize=False)
+        r.RenderBatched(batch, None, 256, 256, synchronize=False)
         out = r.BatchOutputs()
         c = torch.as_tensor(DeviceArray(out.color, (n, 256, 256, 4)), device=dev)
         with torch.cuda.stream(stream):
