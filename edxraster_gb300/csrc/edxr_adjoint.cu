@@ -89,43 +89,45 @@ __device__ __forceinline__ bool pixel_forward(const FrameDesc& f, const DiffMesh
     // The solve cancels heavily (a_k, c_k are the small projected distances of
     // the vertices from the pixel centre, each a difference of O(1) terms), so
     // the clip coordinates, the pixel centre and the solve run in FP64; the
-    // result is rounded to float once.
+    // result is rounded to float once.  FP64 is the slow unit of this GPU:
+    // the products are fused explicitly (fma) and S is inverted once.
     double X[3], Y[3], Wd[3], ac[3], cc[3], bt[3];
     const float* M = f.mvp;
     for (int k = 0; k < 3; k++)
     {
         const double x = s.p[k].x, y = s.p[k].y, z = s.p[k].z;
-        X[k] = (double)M[0] * x + (double)M[1] * y + (double)M[2] * z + (double)M[3];
-        Y[k] = (double)M[4] * x + (double)M[5] * y + (double)M[6] * z + (double)M[7];
-        Wd[k] = (double)M[12] * x + (double)M[13] * y + (double)M[14] * z + (double)M[15];
+        X[k] = fma((double)M[0], x, fma((double)M[1], y, fma((double)M[2], z, (double)M[3])));
+        Y[k] = fma((double)M[4], x, fma((double)M[5], y, fma((double)M[6], z, (double)M[7])));
+        Wd[k] = fma((double)M[12], x, fma((double)M[13], y, fma((double)M[14], z, (double)M[15])));
         s.X[k] = (float)X[k];
         s.Y[k] = (float)Y[k];
         s.W[k] = (float)Wd[k];
     }
     const double rx = (double)px + 0.5, ry = (double)py + 0.5;
     const double* R = f.ndc_from_raster_d;
-    const double u = R[0] * rx + R[1] * ry + R[2];
-    const double v = R[3] * rx + R[4] * ry + R[5];
+    const double u = fma(R[0], rx, fma(R[1], ry, R[2]));
+    const double v = fma(R[3], rx, fma(R[4], ry, R[5]));
     s.u = (float)u;
     s.v = (float)v;
     for (int k = 0; k < 3; k++)
     {
-        ac[k] = X[k] - u * Wd[k];
-        cc[k] = Y[k] - v * Wd[k];
+        ac[k] = fma(-u, Wd[k], X[k]);
+        cc[k] = fma(-v, Wd[k], Y[k]);
         s.ac[k] = (float)ac[k];
         s.cc[k] = (float)cc[k];
     }
-    bt[0] = ac[1] * cc[2] - ac[2] * cc[1];
-    bt[1] = ac[2] * cc[0] - ac[0] * cc[2];
-    bt[2] = ac[0] * cc[1] - ac[1] * cc[0];
+    bt[0] = fma(ac[1], cc[2], -(ac[2] * cc[1]));
+    bt[1] = fma(ac[2], cc[0], -(ac[0] * cc[2]));
+    bt[2] = fma(ac[0], cc[1], -(ac[1] * cc[0]));
     const double S = bt[0] + bt[1] + bt[2];
     if (!(S != 0.0))
         return false;
     s.S = (float)S;
+    const double invS = 1.0 / S;
     for (int k = 0; k < 3; k++)
     {
         s.bt[k] = (float)bt[k];
-        s.b[k] = (float)(bt[k] / S);
+        s.b[k] = (float)(bt[k] * invS);
     }
     s.P = s.b[0] * s.p[0] + s.b[1] * s.p[1] + s.b[2] * s.p[2];
     s.Nraw = s.b[0] * s.n[0] + s.b[1] * s.n[1] + s.b[2] * s.n[2];
