@@ -208,25 +208,6 @@ __global__ void __launch_bounds__(kThreads) k_shade_visible(PassArgs a, uint64_t
     out[i] = make_float4(c.x, c.y, c.z, 1.0f);
 }
 
-__device__ __forceinline__ float block_sum(float v, float* red)
-{
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_down_sync(0xffffffffu, v, o);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __syncthreads();
-    if (lane == 0)
-        red[warp] = v;
-    __syncthreads();
-    float r = 0.0f;
-    if (warp == 0)
-    {
-        r = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0f;
-        for (int o = 16; o > 0; o >>= 1)
-            r += __shfl_down_sync(0xffffffffu, r, o);
-    }
-    return r;  // valid in thread 0
-}
-
 __device__ __forceinline__ void add3(float* g, uint32_t v, V3 d)
 {
     if (!g)
@@ -239,7 +220,7 @@ __device__ __forceinline__ void add3(float* g, uint32_t v, V3 d)
 __global__ void __launch_bounds__(kThreads) k_backward(PassArgs a, uint64_t total, DiffMesh m, const float4* grad,
                                                        DiffGrads g)
 {
-    __shared__ float red[kThreads / 32];
+    __shared__ float red[5 * (kThreads / 32)];
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     V3 dl = v3(0.f, 0.f, 0.f);
     float dks = 0.0f, dshin = 0.0f;
@@ -316,13 +297,30 @@ __global__ void __launch_bounds__(kThreads) k_backward(PassArgs a, uint64_t tota
                 }
         }
     }
-    // block-reduce the five global gradients, accumulate in double
-    const float vals[5] = { dl.x, dl.y, dl.z, dks, dshin };
+    // block-reduce the five global gradients together (one barrier),
+    // accumulate in double
+    float vals[5] = { dl.x, dl.y, dl.z, dks, dshin };
+#pragma unroll
     for (int q = 0; q < 5; q++)
+        for (int o = 16; o > 0; o >>= 1)
+            vals[q] += __shfl_down_sync(0xffffffffu, vals[q], o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < 5; q++)
+            red[q * (kThreads / 32) + warp] = vals[q];
+    __syncthreads();
+    if (warp == 0)
     {
-        const float r = block_sum(vals[q], red);
-        if (threadIdx.x == 0 && r != 0.0f)
-            atomicAdd(g.scratch + q, (double)r);
+#pragma unroll
+        for (int q = 0; q < 5; q++)
+        {
+            float r = lane < kThreads / 32 ? red[q * (kThreads / 32) + lane] : 0.0f;
+            for (int o = 16; o > 0; o >>= 1)
+                r += __shfl_down_sync(0xffffffffu, r, o);
+            if (lane == 0 && r != 0.0f)
+                atomicAdd(g.scratch + q, (double)r);
+        }
     }
 }
 
