@@ -117,11 +117,16 @@ struct SmallTiles
 __device__ __forceinline__ uint32_t small_tiles(const PassArgs& a, const FrameDesc& f, const RTri& t, const BinGeom& g,
                                                SmallTiles& st)
 {
-    // with several samples per pixel a sample off the centre may be covered:
-    // keep the reference's quad-aligned region
-    const bool wf = a.msaa_log2 == 0 && wrap_free(t);
-    const int x0 = max(wf ? g.cx0 : g.bbx0 & ~1, 0), x1 = min(wf ? g.cx1 : g.bbx1 | 1, f.width - 1);
-    const int y0 = max(wf ? g.cy0 : g.bby0 & ~1, 0), y1 = min(wf ? g.cy1 : g.bby1 | 1, f.height - 1);
+    // Without wraparound only points inside the vertices' bounding box can be
+    // covered: with one sample per pixel the pixels whose centre is in it,
+    // with several (each inside its own pixel) the pixels the box overlaps.
+    // Otherwise the reference's quad-aligned region.
+    const bool wfree = wrap_free(t);
+    const bool tight = a.msaa_log2 == 0 && wfree, box = a.msaa_log2 != 0 && wfree;
+    const int x0 = max(tight ? g.cx0 : box ? g.bbx0 : g.bbx0 & ~1, 0);
+    const int x1 = min(tight ? g.cx1 : box ? g.bbx1 : g.bbx1 | 1, f.width - 1);
+    const int y0 = max(tight ? g.cy0 : box ? g.bby0 : g.bby0 & ~1, 0);
+    const int y1 = min(tight ? g.cy1 : box ? g.bby1 : g.bby1 | 1, f.height - 1);
     if (x0 > x1 || y0 > y1)
         return 0;
     st.tx0 = x0 >> kTileLog2;
@@ -1191,8 +1196,13 @@ __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uin
         // when no edge function can wrap (no other centre can be covered)
         const int minx = min(t.v0x, min(t.v1x, t.v2x)), maxx = max(t.v0x, max(t.v1x, t.v2x));
         const int miny = min(t.v0y, min(t.v1y, t.v2y)), maxy = max(t.v0y, max(t.v1y, t.v2y));
-        const int bbx0 = wf ? centre_lo(minx) : (minx >> 4) & ~1, bbx1 = wf ? centre_hi(maxx) : (maxx >> 4) | 1;
-        const int bby0 = wf ? centre_lo(miny) : (miny >> 4) & ~1, bby1 = wf ? centre_hi(maxy) : (maxy >> 4) | 1;
+        // with several samples, each inside its own pixel (offsets -8..7 in
+        // 1/16 pixel): the pixels the wrap-free triangle's box overlaps
+        const bool box = MS && wfree;
+        const int bbx0 = wf ? centre_lo(minx) : box ? minx >> 4 : (minx >> 4) & ~1;
+        const int bbx1 = wf ? centre_hi(maxx) : box ? maxx >> 4 : (maxx >> 4) | 1;
+        const int bby0 = wf ? centre_lo(miny) : box ? miny >> 4 : (miny >> 4) & ~1;
+        const int bby1 = wf ? centre_hi(maxy) : box ? maxy >> 4 : (maxy >> 4) | 1;
         lx0 = max(0, bbx0 - (tileX << 4));
         lx1 = min(15, bbx1 - (tileX << 4));
         ly0 = max(0, bby0 - (tileY << 4));
