@@ -1613,7 +1613,9 @@ static __device__ __noinline__ void write_pixel_ms(const PassArgs& a, const Fram
     const int level = a.msaa_log2;
     const uint64_t plane = a.total_pixels;
     float acc[4] = { 0.f, 0.f, 0.f, 0.f };
-    uint32_t last = kNoTriangle, c8[3] = { 0u, 0u, 0u };
+    uint32_t last = kNoTriangle;
+    float cf[3] = { 0.f, 0.f, 0.f };  // the winner's 8-bit colour / 255
+    RTri t;                            // the record of `last`
     for (int s = 0; s < S; s++)
     {
         const uint32_t r = ri[s];
@@ -1623,23 +1625,24 @@ static __device__ __noinline__ void write_pixel_ms(const PassArgs& a, const Fram
             a.tri_id[s * plane + pix] = kNoTriangle;
             continue;
         }
-        const RTri t = a.rtris[r];
+        if (r != last)
+        {
+            t = a.rtris[r];
+            float L0, L1;
+            depth_at(t, (px << 4) + 8, (py << 4) + 8, L0, L1);
+            const float3 c = shade_fragment(f, t, a.polys, L0, L1, px, py);
+            cf[0] = fdiv((float)to_byte(c.x), 255.0f);
+            cf[1] = fdiv((float)to_byte(c.y), 255.0f);
+            cf[2] = fdiv((float)to_byte(c.z), 255.0f);
+            last = r;
+        }
         const int o = sample_offset(level, s);
         float L0, L1;
         a.depth[s * plane + pix] = depth_at(t, (px << 4) + 8 + o, (py << 4) + 8 + o, L0, L1);
         a.tri_id[s * plane + pix] = t.order >> 4;
-        if (r != last)
-        {
-            depth_at(t, (px << 4) + 8, (py << 4) + 8, L0, L1);
-            const float3 c = shade_fragment(f, t, a.polys, L0, L1, px, py);
-            c8[0] = to_byte(c.x);
-            c8[1] = to_byte(c.y);
-            c8[2] = to_byte(c.z);
-            last = r;
-        }
 #pragma unroll
         for (int q = 0; q < 3; q++)
-            acc[q] = fadd(acc[q], fdiv((float)c8[q], 255.0f));
+            acc[q] = fadd(acc[q], cf[q]);
         acc[3] = fadd(acc[3], 1.0f);
     }
     const float inv = fdiv(1.0f, (float)S);
