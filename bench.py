@@ -564,7 +564,8 @@ def run_gpu(args, world, rank, local):
     traffic = traffic_from_profiles(args.workload)
     line = {
         "metric": "Mtris/s", "value": value, "unit": "Mtris/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "ms_per_step_median": statistics.median(per),
+        "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic (seeded scene generators)",
         "config": {"workload": args.workload, "description": name, "triangles": sc.mesh.nt, "width": W,
                    "height": H, "l2": "512 MiB write between timed frames",
