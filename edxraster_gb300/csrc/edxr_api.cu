@@ -958,7 +958,7 @@ edxr_status edxr_get_stats(edxr_renderer* r, edxr_stats* st)
     if (s != EDXR_OK)
         return s;
     st->raster_triangles = r->status_host->raster_tris;
-    st->bin_entries = r->status_host->bins_needed;
+    st->bin_entries = r->status_host->bin_entries;
     st->bin_capacity = r->bin_capacity;
     st->rerenders = r->rerenders;
     st->tile_size = kTileSize;

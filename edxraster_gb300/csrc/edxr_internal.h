@@ -33,7 +33,18 @@ __host__ __device__ constexpr uint32_t scan_blocks(uint64_t tiles)
 {
     return (uint32_t)((tiles + kScanBlock - 1) / kScanBlock);
 }
-constexpr int kCounters = 16;  // words of PassArgs::counters
+// The unsorted bin list is kBinStripes regions of bin_capacity / kBinStripes
+// slots, each filled through its own counter (one 128-byte line apart, from
+// word kStripeBase of PassArgs::counters): word 0 the region's used slots,
+// word 1 the unclipped triangles that survived setup in warps of that
+// stripe (statistics).  Warps append to stripe (warp index mod kBinStripes),
+// so no block-wide barrier is needed to keep one counter from being the
+// single address every warp of the grid contends for.
+constexpr int kBinStripes = 32;
+constexpr int kStripeStride = 32;
+constexpr int kStripeBase = 16;
+constexpr int kCounters = kStripeBase + kBinStripes * kStripeStride;  // words of PassArgs::counters
+__host__ __device__ constexpr uint64_t stripe_slots(uint64_t bin_capacity) { return bin_capacity / kBinStripes; }
 // Work items of a pass: one per tile plus one per kItemEntries bin entries.
 constexpr uint64_t item_capacity(uint64_t tiles, uint64_t bin_capacity) { return tiles + bin_capacity / kItemEntries + 1; }
 // 3 + one vertex per clip plane is 9 in exact arithmetic; rounding on nearly
@@ -113,11 +124,12 @@ struct DeviceStatus
 {
     uint32_t overflow;       // bins needed more than the capacity
     uint32_t error;          // EDXR_ERR_TIMEOUT and similar
-    uint64_t bins_needed;    // padded bin entries this frame
+    uint64_t bins_needed;    // bin-list capacity this frame needs (padded bins; the fullest stripe x stripes)
     uint32_t raster_tris;    // needed (may exceed the capacity)
     uint32_t clipped_polys;  // needed
     uint32_t big_tris;       // needed
     uint32_t rtri_slots;     // raster-triangle slots needed: input triangles + fan pieces
+    uint64_t bin_entries;    // (triangle, tile) entries binned this frame
 };
 
 // Tunables of one pass (edxr_set_tuning; chosen by the autotuner).
@@ -155,9 +167,9 @@ struct PassArgs
     uint32_t* big_list;      // raster triangles with many tiles, binned by whole blocks
     uint32_t big_capacity;
     uint32_t* counters;      // [0] fan-piece slots, [2] big tris, [3] raster work queue, [4] clip list,
-                             // [5] unsorted bin list slots, [6] heavy raster work items, [7] light ones,
-                             // [8] scan block tickets, [10] unclipped surviving triangles,
-                             // [11] surviving fan pieces (kCounters words)
+                             // [6] heavy raster work items, [7] light ones, [8] scan block tickets,
+                             // [11] surviving fan pieces, [kStripeBase + r * kStripeStride] stripe r of the
+                             // unsorted bin list (kCounters words)
     unsigned long long* scan_status;  // per scan block (scan_blocks(total_tiles) words)
     uint4* items;            // raster work items (tile | split flag, first entry, end entry, 0), one per
                              // kItemEntries-entry slice: heavy ones from the front, light ones from the back

@@ -69,8 +69,9 @@ __global__ void k_clear(PassArgs a)
         a.tile_zocc[i] = 0xFFFFFFFFu;
         a.tile_cursor[i] = 0;
     }
-    if (blockIdx.x == 0 && threadIdx.x < kCounters)
-        a.counters[threadIdx.x] = 0;
+    if (blockIdx.x == 0)
+        for (int i = (int)threadIdx.x; i < kCounters; i += (int)blockDim.x)
+            a.counters[i] = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < scan_blocks(a.total_tiles); i += stride)
         a.scan_status[i] = 0ull;
     if (blockIdx.x == 0 && threadIdx.x == 0)
@@ -81,6 +82,7 @@ __global__ void k_clear(PassArgs a)
         a.status->raster_tris = 0;
         a.status->clipped_polys = 0;
         a.status->big_tris = 0;
+        a.status->bin_entries = 0;
     }
 }
 
@@ -137,19 +139,35 @@ __device__ __forceinline__ uint32_t small_tiles(const PassArgs& a, const FrameDe
 }
 
 // Counts a small triangle's entries in their tiles and keeps them in the
-// unsorted list from `slot` on (the caller reserved their number).
+// unsorted list from `slot` on, up to its stripe's end (the caller reserved
+// their number; entries past the end are dropped, the frame overflows).
 __device__ __forceinline__ void bin_small(const PassArgs& a, const FrameDesc& f, uint32_t ri, const SmallTiles& st,
-                                          uint32_t slot)
+                                          uint64_t slot, uint64_t end)
 {
     for (int ty = st.ty0; ty <= st.ty1; ty++)
         for (int tx = st.tx0; tx <= st.tx1; tx++)
         {
             const uint32_t tile = f.tile_base + (uint32_t)(ty * f.tdx + tx);
             bin_count_tile(a, tile);
-            if (slot < a.bin_capacity)
+            if (slot < end)
                 a.bin_tmp[slot] = make_uint2(tile, (ri << 2) | kDecisionFine);
             slot++;
         }
+}
+
+// Stripe of the unsorted bin list a warp appends to, its fill counter and
+// its first slot.
+__device__ __forceinline__ uint32_t warp_stripe()
+{
+    return ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % (uint32_t)kBinStripes;
+}
+__device__ __forceinline__ uint32_t* stripe_counter(const PassArgs& a, uint32_t r)
+{
+    return a.counters + kStripeBase + r * kStripeStride;
+}
+__device__ __forceinline__ uint64_t stripe_begin(const PassArgs& a, uint32_t r)
+{
+    return (uint64_t)r * stripe_slots(a.bin_capacity);
 }
 
 // A big triangle (bounding box over more than 2x2 reference tiles) goes to
@@ -200,10 +218,8 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, int n)
 // contends for.
 __global__ void __launch_bounds__(256, 6) k_setup(PassArgs a)
 {
-    __shared__ uint32_t s_warp[8], s_went[8];
-    __shared__ uint32_t s_base[3];
     const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31;
     uint32_t fi = 0, tri = 0;
     int nOut = 0;
     bool straddle = false, big = false;
@@ -262,65 +278,42 @@ __global__ void __launch_bounds__(256, 6) k_setup(PassArgs a)
             straddle = (k0 | k1 | k2) != 0 && !(k0 & k1 & k2);
         }
     }
-    // block-wide exclusive scans of (raster triangles, queued triangles),
-    // packed in the low and high halves of one word (each at most 256), and
-    // of the bin entries
-    const uint32_t packed = (uint32_t)nOut | ((straddle ? 1u : 0u) << 16);
-    uint32_t incl = packed, eincl = nent;
+    // warp-wide exclusive scans of the queued triangles and of the bin
+    // entries; one atomic per warp on the clip queue (few warps have any)
+    // and on the warp's stripe of the unsorted list
+    uint32_t qincl = straddle ? 1u : 0u, eincl = nent;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1)
     {
-        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        const uint32_t v = __shfl_up_sync(0xffffffffu, qincl, o);
         const uint32_t ve = __shfl_up_sync(0xffffffffu, eincl, o);
         if (lane >= (uint32_t)o)
         {
-            incl += v;
+            qincl += v;
             eincl += ve;
         }
     }
+    const uint32_t stripe = warp_stripe();
+    const uint32_t survivors = __popc(__ballot_sync(0xffffffffu, nOut != 0));
+    uint32_t qbase = 0, ebase = 0;
     if (lane == 31)
     {
-        s_warp[warp] = incl;
-        s_went[warp] = eincl;
+        if (survivors)
+            atomicAdd(stripe_counter(a, stripe) + 1, survivors);  // statistics
+        qbase = qincl ? atomicAdd(&a.counters[4], qincl) : 0u;
+        ebase = eincl ? atomicAdd(stripe_counter(a, stripe), eincl) : 0u;
     }
-    __syncthreads();
-    if (warp == 0)
-    {
-        const uint32_t w = lane < 8 ? s_warp[lane] : 0u, we = lane < 8 ? s_went[lane] : 0u;
-        uint32_t wi = w, wei = we;
-#pragma unroll
-        for (int o = 1; o < 8; o <<= 1)
-        {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, wi, o);
-            const uint32_t ve = __shfl_up_sync(0xffffffffu, wei, o);
-            if (lane >= (uint32_t)o)
-            {
-                wi += v;
-                wei += ve;
-            }
-        }
-        if (lane < 8)
-        {
-            s_warp[lane] = wi - w;
-            s_went[lane] = wei - we;
-        }
-        if (lane == 7)
-        {
-            s_base[0] = (wi & 0xFFFFu) ? atomicAdd(&a.counters[10], wi & 0xFFFFu) : 0u;  // survivors (statistics)
-            s_base[1] = (wi >> 16) ? atomicAdd(&a.counters[4], wi >> 16) : 0u;
-            s_base[2] = wei ? atomicAdd(&a.counters[5], wei) : 0u;
-        }
-    }
-    __syncthreads();
-    const uint32_t excl = s_warp[warp] + incl - packed;
+    qbase = __shfl_sync(0xffffffffu, qbase, 31);
+    ebase = __shfl_sync(0xffffffffu, ebase, 31);
     if (straddle)
     {
-        const uint32_t q = s_base[1] + (excl >> 16);
+        const uint32_t q = qbase + qincl - 1u;
         if (q < a.poly_capacity)
             a.clip_list[q] = gi;
     }
     // an unclipped triangle's record sits at its flattened index
-    const uint32_t slot = s_base[2] + s_went[warp] + eincl - nent;
+    const uint64_t sbegin = stripe_begin(a, stripe);
+    const uint64_t slot = sbegin + ebase + eincl - nent;
     if (nOut)
     {
         t.order = tri << 4;
@@ -330,7 +323,7 @@ __global__ void __launch_bounds__(256, 6) k_setup(PassArgs a)
     }
     bin_big_append(a, gi, nOut && big);
     if (nOut && nent)
-        bin_small(a, a.frames[fi], gi, st, slot);
+        bin_small(a, a.frames[fi], gi, st, slot, sbegin + stripe_slots(a.bin_capacity));
 }
 
 // Clipping of the queued triangles (Clipper.h:107-171): Sutherland-Hodgman,
@@ -472,9 +465,11 @@ __device__ __forceinline__ void clip_piece(const PassArgs& a, bool has, uint32_t
     if ((threadIdx.x & 31) == 0 && kept_lanes)
         atomicAdd(&a.counters[11], (uint32_t)__popc(kept_lanes));
     bin_big_append(a, ri, big);
-    const uint32_t slot = warp_append(&a.counters[5], (int)nent);
+    const uint32_t stripe = warp_stripe();
+    const uint64_t sbegin = stripe_begin(a, stripe);
+    const uint64_t slot = sbegin + warp_append(stripe_counter(a, stripe), (int)nent);
     if (nent)
-        bin_small(a, f, ri, st, slot);
+        bin_small(a, f, ri, st, slot, sbegin + stripe_slots(a.bin_capacity));
 }
 
 // Vertex of lane `src` (within the 16-lane group) of every lane's group.
@@ -710,21 +705,49 @@ __global__ void __launch_bounds__(kClipThreads) k_clip(PassArgs a)
 // slots are skipped.
 __global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
 {
-    const uint32_t n = *(volatile uint32_t*)&a.counters[5];
-    const uint32_t m = (uint32_t)min((uint64_t)n, a.bin_capacity);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounds = (m + stride - 1) / stride;
+    // the filled parts of the stripes (slots past a stripe's end were
+    // dropped: overflow), numbered one after another
+    __shared__ uint32_t s_first[kBinStripes + 1];
+    const uint64_t R = stripe_slots(a.bin_capacity);
     const uint32_t lane = threadIdx.x & 31;
-    for (uint32_t r = 0; r < rounds; r++)
+    if (threadIdx.x < 32)
     {
-        const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        const uint2 e = i < m ? a.bin_tmp[i] : make_uint2(kEmptySlot, 0u);
+        static_assert(kBinStripes == 32, "one lane per stripe");
+        const uint32_t m = (uint32_t)min((uint64_t)*(volatile uint32_t*)stripe_counter(a, lane), R);
+        uint32_t incl = m;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += v;
+        }
+        s_first[lane] = incl - m;
+        if (lane == 31)
+            s_first[32] = incl;
+    }
+    __syncthreads();
+    const uint32_t total = s_first[kBinStripes];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (total + stride - 1) / stride;
+    for (uint32_t rd = 0; rd < rounds; rd++)
+    {
+        const uint32_t j = rd * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        uint2 e = make_uint2(kEmptySlot, 0u);
+        if (j < total)
+        {
+            // stripe of entry j: the last one starting at or before it
+            uint32_t r = 0;
+#pragma unroll
+            for (uint32_t st = 16; st >= 1; st >>= 1)
+                if (s_first[r + st] <= j) r += st;
+            e = a.bin_tmp[(uint64_t)r * R + (j - s_first[r])];
+        }
         uint32_t base = 0;
         if (a.vrecs)
         {
-            // a mesh with shared vertices: neighbouring lanes hold entries of
-            // neighbouring triangles, interleaved over the same few tiles;
-            // all lanes with equal tiles share one atomic
+            // a mesh with shared vertices: neighbouring lanes hold entries
+            // of neighbouring triangles, interleaved over the same few
+            // tiles; all lanes with equal tiles share one atomic
             const uint32_t peers = __match_any_sync(0xffffffffu, e.x);
             const int leader = __ffs(peers) - 1;
             if ((int)lane == leader && e.x != kEmptySlot)
@@ -733,8 +756,8 @@ __global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
         }
         else
         {
-            // a triangle soup: lanes rarely share a tile, except in runs of
-            // consecutive lanes, which share one atomic
+            // a triangle soup: lanes rarely share a tile, except in runs
+            // of consecutive lanes, which share one atomic
             const uint32_t prev = __shfl_up_sync(0xffffffffu, e.x, 1);
             const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0 || e.x != prev);
             const uint32_t upto = 0xffffffffu >> (31 - lane);  // lanes 0..lane
@@ -784,10 +807,14 @@ __global__ void __launch_bounds__(256, 4) k_bin_big(PassArgs a)
     const uint32_t nb = min(*(volatile uint32_t*)&a.counters[2], a.big_capacity);
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    uint32_t cbase = 0, cleft = 0;  // the warp's current chunk
+    // the warp's current chunk of its stripe of the unsorted list
+    const uint32_t stripe = warp_stripe();
+    const uint64_t send = stripe_begin(a, stripe) + stripe_slots(a.bin_capacity);
+    uint64_t cbase = 0;
+    uint32_t cleft = 0;
     auto mark_empty = [&]() {
         for (uint32_t k = lane; k < cleft; k += 32)
-            if (cbase + k < a.bin_capacity)
+            if (cbase + k < send)
                 a.bin_tmp[cbase + k] = make_uint2(kEmptySlot, 0u);
     };
     // batches of up to 32 triangles, small enough that every warp gets one
@@ -860,11 +887,11 @@ __global__ void __launch_bounds__(256, 4) k_bin_big(PassArgs a)
                 mark_empty();
                 uint32_t nbase = 0;
                 if (lane == 0)
-                    nbase = atomicAdd(&a.counters[5], kBigChunk);
-                cbase = __shfl_sync(0xffffffffu, nbase, 0);
+                    nbase = atomicAdd(stripe_counter(a, stripe), kBigChunk);
+                cbase = stripe_begin(a, stripe) + __shfl_sync(0xffffffffu, nbase, 0);
                 cleft = kBigChunk;
             }
-            uint32_t pos = cbase + (uint32_t)(cincl - cnt);
+            uint64_t pos = cbase + (uint32_t)(cincl - cnt);
 #pragma unroll
             for (int q = 0; q < 4; q++)
             {
@@ -875,7 +902,7 @@ __global__ void __launch_bounds__(256, 4) k_bin_big(PassArgs a)
                 atomicAdd(&a.tile_count[tile], 1u);
                 if (d == kDecisionAccept && zocc != 0xFFFFFFFFu)
                     atomicMin(&a.tile_zocc[tile], zocc);
-                if (pos < a.bin_capacity)
+                if (pos < send)
                     a.bin_tmp[pos] = make_uint2(tile, (ri << 2) | d);
                 pos++;
             }
@@ -996,7 +1023,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
     // did not all fit (the unsorted list or the bins overflowed) is rendered
     // again by the host; its tiles are made empty here, so no raster item
     // reads a bin with missing entries or leaves a split tile's keys behind.
-    const bool dropped = *(volatile uint32_t*)&a.counters[5] > a.bin_capacity;
+    const bool dropped =
+        __syncthreads_or(threadIdx.x < (uint32_t)kBinStripes &&
+                         *(volatile uint32_t*)stripe_counter(a, threadIdx.x) > stripe_slots(a.bin_capacity)) != 0;
     uint32_t run = prefix + incl - sum;
     uint32_t nheavy = 0, nlight = 0;
     uint32_t start[kScanItems], n[kScanItems];
@@ -1073,10 +1102,19 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
     {
         const uint64_t grand = prefix + total;
         a.tile_offset[a.total_tiles] = (uint32_t)grand;
-        // the unsorted list shares the capacity
-        const uint64_t needed = max(grand, (uint64_t)a.counters[5]);
+        // the unsorted list's stripes share the capacity: the fullest decides
+        uint64_t fullest = 0, entries = 0, survivors = 0;
+        for (int r = 0; r < kBinStripes; r++)
+        {
+            const uint32_t* c = stripe_counter(a, (uint32_t)r);
+            fullest = max(fullest, (uint64_t)c[0]);
+            entries += c[0];
+            survivors += c[1];
+        }
+        const uint64_t needed = max(grand, fullest * kBinStripes);
         a.status->bins_needed = needed;
-        a.status->raster_tris = a.counters[10] + a.counters[11];
+        a.status->bin_entries = entries;
+        a.status->raster_tris = (uint32_t)survivors + a.counters[11];
         a.status->rtri_slots = a.total_tris + a.counters[0];
         a.status->big_tris = a.counters[2];
         if ((uint64_t)a.total_tris + a.counters[0] > a.rtri_capacity)
