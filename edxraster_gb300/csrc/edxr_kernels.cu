@@ -190,8 +190,8 @@ __device__ __forceinline__ void bin_big_append(const PassArgs& a, uint32_t ri, b
 }
 
 
-// Appends n raster triangles for this lane with one atomic per warp; returns
-// the lane's first slot.  Every lane of the warp must call it.
+// Appends n slots for this lane with one atomic per warp on `counter`;
+// returns the lane's first slot.  Every lane of the warp must call it.
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, int n)
 {
     const uint32_t lane = threadIdx.x & 31;
@@ -212,10 +212,9 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, int n)
 // Setup of the triangles that need no clipping (all clip codes zero), one
 // thread per input triangle; triangles that straddle a clip plane are queued
 // for k_clip, triangles outside one plane are dropped (Clipper.h:103-109).
-// A small set-up triangle is binned here as well.  The raster-triangle list,
-// the clip queue and the unsorted bin list are appended to with one atomic
-// per block each: the counters are single addresses every block of the grid
-// contends for.
+// A small set-up triangle is binned here as well.  A set-up triangle's
+// record goes to its own slot (no append); the clip queue and the warp's
+// stripe of the unsorted bin list take one atomic per warp each.
 __global__ void __launch_bounds__(256, 6) k_setup(PassArgs a)
 {
     const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
