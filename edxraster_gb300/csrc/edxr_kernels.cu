@@ -2,7 +2,8 @@
 //
 // One pass renders any number of frames (a frame = one mesh seen by one
 // camera); the plain path is a pass of one frame.  Stages:
-//   k_clear        zero the per-tile counters and work queues
+//   k_clear        zero the per-tile counters and work queues;  Renderer.cpp:120-127
+//                  the vertex stage of shared-vertex meshes
 //   k_setup        clip = MVP * (p, 1), clip codes, fixed-point Shader.h:40-49,
 //   k_clip         setup and the post-pass per input triangle;  Clipper.h:71-189,
 //                  clipping of those that straddle a plane;     RasterTriangle.h:27-153
