@@ -89,6 +89,18 @@ def test_stress_medium(cuda_lib):
     check_against_oracle(scenes.stress_scene(40000, 960, 540, seed=7))
 
 
+@pytest.mark.parametrize("workload", ["terrain", "stress"])
+def test_benchmark_workloads_full_size(cuda_lib, workload):
+    """The benchmark's own scenes at full size (the heightfield's 2,097,152
+    triangles at 1920x1080 with its vertex stage and clipping; the stress
+    scene's 1,000,000 triangles at 3840x2160 with split tiles and occluder
+    bounds): every pixel's winner and depth bit-exact, colour within 1e-5."""
+    sc = {"terrain": lambda: scenes.terrain_scene(1024, 1920, 1080, seed=1),
+          "stress": lambda: scenes.stress_scene(1_000_000, 3840, 2160, seed=7)}[workload]()
+    _, coverage = check_against_oracle(sc)
+    assert coverage > 0.3
+
+
 def deep_clip_scene(n, width, height, seed):
     """Large clip-space triangles that cross several clip planes at once
     (sides, near, far, w < 0): clipped polygons of up to nine vertices."""
