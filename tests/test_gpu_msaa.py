@@ -73,6 +73,20 @@ def test_msaa_clipping_and_split_tiles(cuda_lib):
     check_color(color, o["color"], 4)
 
 
+@pytest.mark.parametrize("workload,lg", [("terrain", 2), ("stress", 1)])
+def test_msaa_benchmark_workloads_full_size(cuda_lib, workload, lg):
+    """The benchmark's full-size scenes with samples: per-sample winners and
+    depths bit-exact (wrap-free triangles binned and rasterized over the
+    pixels their box overlaps, tile occluder bounds over samples)."""
+    sc = {"terrain": lambda: scenes.terrain_scene(1024, 1920, 1080, seed=1),
+          "stress": lambda: scenes.stress_scene(1_000_000, 3840, 2160, seed=7)}[workload]()
+    color, depth, tid, _ = render_ms(sc, lg)
+    o = pyoracle.render_oracle(sc.mesh, sc.view, depth_func=sc.view.depth_func, msaa_log2=lg)
+    assert not mismatch_report("triangle id", tid, o["id"])
+    assert not mismatch_report("depth", depth.view(np.uint32), o["depth"].view(np.uint32))
+    check_color(color, o["color"], 1 << lg)
+
+
 def test_msaa_back_buffer_is_the_resolve(cuda_lib):
     sc = scenes.sphere_scene(160, 96)
     color, depth, tid, back = render_ms(sc, 3)
