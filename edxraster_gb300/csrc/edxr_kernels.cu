@@ -1335,7 +1335,7 @@ struct PixelOut
     uint32_t* tri_id;
 };
 
-static __device__ __noinline__ void write_pixel(const PixelOut a, const FrameDesc& f, uint32_t ri, uint64_t pix, int px,
+static __device__ __forceinline__ void write_pixel(const PixelOut a, const FrameDesc& f, uint32_t ri, uint64_t pix, int px,
                                                 int py)
 {
     if (ri == kNoTriangle)
@@ -1645,7 +1645,7 @@ __device__ __forceinline__ float depth_at(const RTri& t, int x, int y, float& L0
 // winner's colour shaded at the pixel centre as 8 bits (Renderer.cpp:
 // 295-350), the samples are averaged in float (alpha 1 per covered sample,
 // 0 for the clear value).  Samples that share a winner share its shading.
-static __device__ __noinline__ void write_pixel_ms(const PassArgs& a, const FrameDesc& f, const uint32_t* ri, int S,
+static __device__ __forceinline__ void write_pixel_ms(const PassArgs& a, const FrameDesc& f, const uint32_t* ri, int S,
                                                    uint64_t pix, int px, int py)
 {
     const int level = a.msaa_log2;
