@@ -1324,8 +1324,8 @@ __device__ __forceinline__ uint32_t raster_triangle_of(const PassArgs& a, uint32
 // The one write of a pixel (Renderer::FragmentProcessing / UpdateFrameBuffer,
 // Renderer.cpp:272-350, shade every fragment and keep the last; only the
 // winner is shaded here): its barycentrics and depth are recomputed exactly
-// (RasterTriangle.h:324-337), then interpolated and shaded.  Not inlined, so
-// the shading's registers do not weigh on the raster loop.
+// (RasterTriangle.h:324-337), then interpolated and shaded.  Inlined: a
+// call per pixel cost more than the registers it spills in the raster loop.
 struct PixelOut
 {
     const RTri* rtris;
