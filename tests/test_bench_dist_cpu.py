@@ -63,3 +63,21 @@ def test_reference_arm_runs_on_rank_zero_only(capsys):
     args = argparse.Namespace(workload="sphere", steps=1, warmup=3)
     assert bench.run_reference(args, 2, 1) == 0
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_line_keeps_the_contract(capsys):
+    """The reference arm's one JSON line on rank 0: the metric of the GPU arm,
+    the CPU implementation timed (the oracle port here), e2e without copies."""
+    import json
+    sys.path.insert(0, ROOT)
+    import bench
+    args = argparse.Namespace(workload="sphere", steps=2, warmup=3)
+    assert bench.run_reference(args, 1, 0) == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["metric"] == "Mtris/s" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] in ("port", "reference") and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    assert line["config"]["workload"] == "sphere"
