@@ -1546,21 +1546,15 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
         }
         if (shade)
         {
-            // winners' raster triangles first (independent loads), then shading
-            uint32_t ri[8];
-#pragma unroll
-            for (int k = 0; k < 8; k++)
-            {
-                const uint32_t low = (uint32_t)key[lane + 32 * k];
-                ri[k] = raster_triangle_of(a, less ? low : ~low, nr);
-            }
 #pragma unroll 1
             for (int k = 0; k < 8; k++)
             {
                 const int p = (int)lane + 32 * k;
                 const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
+                const uint32_t low = (uint32_t)key[p];
+                const uint32_t ri = raster_triangle_of(a, less ? low : ~low, nr);
                 if (px < f.width && py < f.height)
-                    write_pixel(out, f, ri[k], f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px, px, py);
+                    write_pixel(out, f, ri, f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px, px, py);
             }
         }
         __syncwarp();
