@@ -10,7 +10,7 @@ import pytest
 from edxraster_gb300 import renderer as R
 from edxraster_gb300 import scenes
 from oracle import pyoracle
-from _scenes import golden_names, load_golden, mismatch_report
+from _scenes import deep_clip_scene, golden_names, load_golden, mismatch_report
 
 pytestmark = pytest.mark.gpu
 COLOR_TOL = 1e-5
@@ -99,25 +99,6 @@ def test_benchmark_workloads_full_size(cuda_lib, workload):
           "stress": lambda: scenes.stress_scene(1_000_000, 3840, 2160, seed=7)}[workload]()
     _, coverage = check_against_oracle(sc)
     assert coverage > 0.3
-
-
-def deep_clip_scene(n, width, height, seed):
-    """Large clip-space triangles that cross several clip planes at once
-    (sides, near, far, w < 0): clipped polygons of up to nine vertices."""
-    rng = np.random.default_rng(seed)
-    xy = rng.uniform(-8.0, 8.0, size=(n, 3, 2))
-    w = rng.uniform(-1.0, 6.0, size=(n, 3, 1))
-    pos = np.concatenate([xy, w], -1).reshape(-1, 3).astype(np.float32)  # object = (x_clip, y_clip, w)
-    nrm = rng.normal(size=(3 * n, 3))
-    nrm /= np.linalg.norm(nrm, axis=-1, keepdims=True)
-    alb = rng.uniform(0.0, 1.0, size=(3 * n, 3))
-    mesh = scenes.Mesh(pos, nrm.astype(np.float32), alb.astype(np.float32), np.zeros((3 * n, 2), np.float32),
-                       np.arange(3 * n, dtype=np.uint32).reshape(n, 3))
-    proj = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, scenes.STRESS_A, scenes.STRESS_B], [0, 0, 1, 0]],
-                    np.float32)
-    view = scenes.View(width, height, np.eye(4, dtype=np.float32), proj, scenes.raster_matrix(width, height),
-                       np.array([0.3, 0.5, -0.81], np.float32) / np.linalg.norm([0.3, 0.5, -0.81]))
-    return scenes.Scene("deep_clip", mesh, view)
 
 
 @pytest.mark.parametrize("n,width,height", [(400, 160, 120), (16000, 48, 32)])

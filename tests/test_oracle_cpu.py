@@ -10,7 +10,7 @@ import pytest
 
 from edxraster_gb300 import scenes
 from oracle import pyoracle
-from _scenes import golden_names, load_golden, load_golden_ms, mismatch_report
+from _scenes import deep_clip_scene, golden_names, load_golden, load_golden_ms, mismatch_report
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -74,9 +74,12 @@ def _live_cases():
     yield scenes.stress_scene(3000, 320, 240, seed=3, max_area=5e3), True
     yield scenes.terrain_scene(40, 160, 96, seed=5), True
     yield scenes.sphere_scene(200, 120, slices=12, stacks=9), True
+    # triangles crossing several clip planes at once, w < 0 included
+    yield deep_clip_scene(300, 96, 72, seed=21), True
+    yield deep_clip_scene(40, 96, 72, seed=22), False
 
 
-@pytest.mark.parametrize("case", range(6))
+@pytest.mark.parametrize("case", range(8))
 def test_oracle_matches_reference_live(case):
     if pyoracle.reference_lib() is None:
         pytest.skip("reference sources not available here")
