@@ -49,6 +49,20 @@ def test_oracle_matches_reference_live_msaa(lg):
     assert o["fragments"] == r["fragments"]
 
 
+@pytest.mark.parametrize("lg,hier", [(2, True), (3, False)])
+def test_oracle_matches_reference_live_msaa_clipping(lg, hier):
+    if pyoracle.reference_lib() is None:
+        pytest.skip("reference sources not available here")
+    sc = deep_clip_scene(120, 64, 48, seed=30 + lg)
+    r = pyoracle.render_reference_ms(sc.mesh, sc.view, lg, hierarchical=hier)
+    o = pyoracle.render_oracle(sc.mesh, sc.view, hierarchical=hier, depth_func=scenes.DEPTH_LEQUAL, threads=2,
+                               with_color=False, msaa_log2=lg)
+    assert (r["id"] != 0xFFFFFFFF).any()
+    assert np.array_equal(o["id"], r["id"])
+    assert np.array_equal(o["depth"].view(np.uint32), r["depth"].view(np.uint32))
+    assert o["fragments"] == r["fragments"]
+
+
 def test_msaa_resolve_arithmetic():
     """The resolved colour of a pixel is the float average of its samples'
     8-bit colours; a pixel whose samples all see one triangle resolves to
