@@ -10,6 +10,7 @@ import pytest
 
 from edxraster_gb300 import scenes
 from oracle import pyoracle
+import _scenes
 from _scenes import deep_clip_scene, golden_names, load_golden, load_golden_ms, mismatch_report
 
 
@@ -100,6 +101,32 @@ def test_oracle_matches_reference_live(case):
     sc, hier = list(_live_cases())[case]
     r = pyoracle.render_reference(sc.mesh, sc.view, hierarchical=hier)
     o = pyoracle.render_oracle(sc.mesh, sc.view, hierarchical=hier, depth_func=scenes.DEPTH_LEQUAL, threads=2)
+    assert not mismatch_report("id", o["id"], r["id"])
+    assert not mismatch_report("depth", o["depth"].view(np.uint32), r["depth"].view(np.uint32))
+    assert o["fragments"] == r["fragments"]
+
+
+EDGE_SCENES = {
+    "int32_wraparound_4k": lambda: _scenes.wraparound_4k_scene(0),
+    "every_clip_plane": _scenes.every_clip_plane_scene,
+    "far_plane_and_behind": _scenes.far_and_behind_scene,
+    "degenerate_and_non_finite": _scenes.degenerate_scene,
+    "coplanar_ties": _scenes.coplanar_scene,
+}
+
+
+@pytest.mark.parametrize("hier", [True, False])
+@pytest.mark.parametrize("name", sorted(EDGE_SCENES))
+def test_oracle_matches_reference_on_edge_scenes(name, hier):
+    """The scenes of the GPU robustness tests, so that the GPU's agreement
+    with the oracle there is agreement with the reference's own code."""
+    if pyoracle.reference_lib() is None:
+        pytest.skip("reference sources not available here")
+    sc = EDGE_SCENES[name]()
+    r = pyoracle.render_reference(sc.mesh, sc.view, hierarchical=hier)
+    o = pyoracle.render_oracle(sc.mesh, sc.view, hierarchical=hier, depth_func=scenes.DEPTH_LEQUAL, threads=2,
+                               with_color=False)
+    assert (r["id"] != 0xFFFFFFFF).any()
     assert not mismatch_report("id", o["id"], r["id"])
     assert not mismatch_report("depth", o["depth"].view(np.uint32), r["depth"].view(np.uint32))
     assert o["fragments"] == r["fragments"]
