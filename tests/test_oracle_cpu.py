@@ -64,6 +64,24 @@ def test_oracle_matches_reference_live_msaa_clipping(lg, hier):
     assert o["fragments"] == r["fragments"]
 
 
+@pytest.mark.parametrize("scene,lg", [("stress", 2), ("stress", 4), ("stress", 5), ("terrain", 2)])
+def test_oracle_matches_reference_on_msaa_test_scenes(scene, lg):
+    """The LEQUAL scenes of the GPU multisample tests (duplicated triangles,
+    clipping and split horizon tiles) against the reference's own code."""
+    if pyoracle.reference_lib() is None:
+        pytest.skip("reference sources not available here")
+    if scene == "stress":
+        sc = scenes.stress_scene(4000, 160, 120, seed=30 + lg, max_area=3e3, dup_fraction=0.1)
+    else:
+        sc = scenes.terrain_scene(96, 320, 180, seed=4)
+    r = pyoracle.render_reference_ms(sc.mesh, sc.view, lg)
+    o = pyoracle.render_oracle(sc.mesh, sc.view, depth_func=scenes.DEPTH_LEQUAL, threads=2, with_color=False,
+                               msaa_log2=lg)
+    assert np.array_equal(o["id"], r["id"])
+    assert np.array_equal(o["depth"].view(np.uint32), r["depth"].view(np.uint32))
+    assert o["fragments"] == r["fragments"]
+
+
 def test_msaa_resolve_arithmetic():
     """The resolved colour of a pixel is the float average of its samples'
     8-bit colours; a pixel whose samples all see one triangle resolves to
