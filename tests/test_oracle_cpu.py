@@ -82,6 +82,30 @@ def test_oracle_matches_reference_on_msaa_test_scenes(scene, lg):
     assert o["fragments"] == r["fragments"]
 
 
+BENCH_SCENES = {
+    "terrain": lambda: scenes.terrain_scene(1024, 1920, 1080, seed=1),
+    "stress": lambda: scenes.stress_scene(1_000_000, 3840, 2160, seed=7),
+}
+
+
+@pytest.mark.parametrize("workload,lg", [("terrain", 0), ("stress", 0), ("terrain", 2), ("stress", 1)])
+def test_oracle_matches_reference_on_benchmark_workloads(workload, lg):
+    """The benchmark's workloads at full size (terrain: 2,097,152 triangles at
+    1920x1080; stress: 1,000,000 at 3840x2160), single-sample and with the
+    sample counts of the GPU full-size multisample test."""
+    if pyoracle.reference_lib() is None:
+        pytest.skip("reference sources not available here")
+    sc = BENCH_SCENES[workload]()
+    if lg:
+        r = pyoracle.render_reference_ms(sc.mesh, sc.view, lg)
+    else:
+        r = pyoracle.render_reference(sc.mesh, sc.view)
+    o = pyoracle.render_oracle(sc.mesh, sc.view, depth_func=scenes.DEPTH_LEQUAL, with_color=False, msaa_log2=lg)
+    assert not mismatch_report("id", o["id"].reshape(-1, sc.view.width), r["id"].reshape(-1, sc.view.width))
+    assert np.array_equal(o["depth"].view(np.uint32), r["depth"].view(np.uint32))
+    assert o["fragments"] == r["fragments"]
+
+
 def test_msaa_resolve_arithmetic():
     """The resolved colour of a pixel is the float average of its samples'
     8-bit colours; a pixel whose samples all see one triangle resolves to
