@@ -140,3 +140,27 @@ def coplanar_scene():
         pts = [(c[0] + 0.3 * np.cos(a), c[1] + 0.3 * np.sin(a), 0.5, 1.0) for a in (0.0, -2.1, -4.2)]
         tris.append(pts)
     return clip_space_scene(tris, 256, 192, 2)
+
+
+def occluder_scene():
+    """Screen-covering planes at equal and nearly equal depths, triangles that
+    straddle their depth, small ones just in front and just behind."""
+    rng = np.random.default_rng(5)
+    tris = []
+    for k in range(300):
+        z = float(rng.choice([0.3, 0.3, 0.5, np.nextafter(np.float32(0.3), np.float32(1.0))]))
+        if k % 3 == 0:  # screen-covering quad halves (accepted over whole tiles)
+            quad = [(-1.2, -1.2), (1.2, -1.2), (1.2, 1.2), (-1.2, 1.2)]
+            t1 = [(x, y, z, 1.0) for x, y in (quad[0], quad[2], quad[1])]
+            t2 = [(x, y, z, 1.0) for x, y in (quad[0], quad[3], quad[2])]
+            tris += [t1, t2]
+        else:
+            c = rng.uniform(-0.9, 0.9, size=2)
+            xy = c + rng.uniform(-0.3, 0.3, size=(3, 2))
+            zs = z + rng.uniform(-0.05, 0.05, size=3) * (k % 2)
+            t = [(x, y, float(zz), 1.0) for (x, y), zz in zip(xy, zs)]
+            a = np.cross(np.r_[xy[1] - xy[0], 0], np.r_[xy[2] - xy[0], 0])[2]
+            if a > 0:  # clockwise on screen (raster y points down)
+                t = [t[0], t[2], t[1]]
+            tris.append(t)
+    return clip_space_scene(tris, 160, 128)

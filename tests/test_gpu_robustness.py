@@ -7,8 +7,8 @@ import pytest
 from edxraster_gb300 import renderer as R
 from edxraster_gb300 import scenes
 from oracle import pyoracle
-from _scenes import (clip_space_scene, coplanar_scene, degenerate_scene, every_clip_plane_scene, far_and_behind_scene,
-                     mismatch_report, wraparound_4k_scene)
+from _scenes import (coplanar_scene, degenerate_scene, every_clip_plane_scene, far_and_behind_scene,
+                     mismatch_report, occluder_scene, wraparound_4k_scene)
 
 pytestmark = pytest.mark.gpu
 
@@ -67,25 +67,7 @@ def test_occluders_cull_only_hidden_entries(cuda_lib, depth_func):
     depth.  Planes at equal and nearly equal depths (ties decided by
     submission order), triangles that straddle the occluder's depth, small
     ones in front of and just behind it: all winners as the oracle's."""
-    rng = np.random.default_rng(5)
-    tris = []
-    for k in range(300):
-        z = float(rng.choice([0.3, 0.3, 0.5, np.nextafter(np.float32(0.3), np.float32(1.0))]))
-        if k % 3 == 0:  # screen-covering quad halves (accepted over whole tiles)
-            quad = [(-1.2, -1.2), (1.2, -1.2), (1.2, 1.2), (-1.2, 1.2)]
-            t1 = [(x, y, z, 1.0) for x, y in (quad[0], quad[2], quad[1])]
-            t2 = [(x, y, z, 1.0) for x, y in (quad[0], quad[3], quad[2])]
-            tris += [t1, t2]
-        else:
-            c = rng.uniform(-0.9, 0.9, size=2)
-            xy = c + rng.uniform(-0.3, 0.3, size=(3, 2))
-            zs = z + rng.uniform(-0.05, 0.05, size=3) * (k % 2)
-            t = [(x, y, float(zz), 1.0) for (x, y), zz in zip(xy, zs)]
-            a = np.cross(np.r_[xy[1] - xy[0], 0], np.r_[xy[2] - xy[0], 0])[2]
-            if a > 0:  # clockwise on screen (raster y points down)
-                t = [t[0], t[2], t[1]]
-            tris.append(t)
-    sc = clip_space_scene(tris, 160, 128)
+    sc = occluder_scene()
     sc.view.depth_func = depth_func
     (c, d, t), _ = gpu(sc)
     o = pyoracle.render_oracle(sc.mesh, sc.view, depth_func=depth_func)

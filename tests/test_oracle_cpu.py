@@ -154,6 +154,8 @@ EDGE_SCENES = {
     "far_plane_and_behind": _scenes.far_and_behind_scene,
     "degenerate_and_non_finite": _scenes.degenerate_scene,
     "coplanar_ties": _scenes.coplanar_scene,
+    "occluders": _scenes.occluder_scene,
+    "duplicate_triangles": lambda: scenes.stress_scene(6000, 320, 200, seed=7, max_area=3e3, dup_fraction=0.25),
 }
 
 
