@@ -168,6 +168,30 @@ def job_throughput(world: int, units_per_rank: int, steps: int, total_ms: float)
     return world * units_per_rank * steps / (total_ms / 1e3) / 1e6
 
 
+def workload_config(workload: str, sc, world: int) -> dict:
+    """The `config` of both arms' JSON lines (the GPU arm and the reference arm)."""
+    return {"workload": workload, "description": WORKLOADS[workload][0], "triangles": sc.mesh.nt,
+            "width": sc.view.width, "height": sc.view.height, "l2": "512 MiB write between timed frames",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
+def oracle_parity(mesh, view, color, depth, tid, threads=None, msaa_log2=0):
+    """The GPU frame against the CPU oracle on the same inputs: winning
+    triangle and depth bit for bit, colour as the largest absolute error
+    against the oracle's FP64 shading over covered pixels (with several
+    samples per pixel: the per-sample ids and depths)."""
+    from oracle import pyoracle
+    o = pyoracle.render_oracle(mesh, view, threads=threads or os.cpu_count(), with_color=msaa_log2 == 0,
+                               msaa_log2=msaa_log2)
+    out = {"id_exact": bool(np.array_equal(tid, o["id"])),
+           "depth_exact": bool(np.array_equal(np.asarray(depth).view(np.uint32), o["depth"].view(np.uint32)))}
+    if msaa_log2 == 0:
+        cov = o["id"] != 0xFFFFFFFF
+        out["color_err_max"] = float(np.abs(color[cov, :3] - o["color"][cov, :3]).max()) if cov.any() else 0.0
+    out["covered_pixels"] = int((o["id"] != 0xFFFFFFFF).sum())
+    return out
+
+
 def cpu_oracle_time(sc, threads: int):
     from oracle import pyoracle
     t0 = time.perf_counter()
@@ -175,13 +199,14 @@ def cpu_oracle_time(sc, threads: int):
     return time.perf_counter() - t0
 
 
-def cpu_baseline(sc, frames: int = 1):
-    """The oracle port on this host: best of `frames` full frames."""
+def cpu_baseline(sc, frames: int = 5):
+    """The oracle port on this host: median of `frames` full frames after one warm-up frame."""
     threads = os.cpu_count() or 1
+    cpu_oracle_time(sc, threads)
     times = [cpu_oracle_time(sc, threads) for _ in range(max(1, frames))]
-    t = min(times)
+    t = statistics.median(times)
     return {"value": sc.mesh.nt / t / 1e6, "unit": "Mtris/s", "cores": threads, "kind": "port",
-            "sample": "one full frame of the workload (%d tris, %dx%d) per measurement, best of %d"
+            "sample": "full frames of the workload (%d tris, %dx%d), median of %d after one warm-up frame"
                       % (sc.mesh.nt, sc.view.width, sc.view.height, len(times))}
 
 
@@ -213,8 +238,7 @@ def run_reference(args, world, rank):
         "impl": "reference", "metric": "Mtris/s", "value": value, "unit": "Mtris/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic",
-        "config": {"workload": args.workload, "description": name, "triangles": sc.mesh.nt,
-                   "width": sc.view.width, "height": sc.view.height},
+        "config": workload_config(args.workload, sc, world),
         "gpix_per_s": sc.view.width * sc.view.height / t / 1e9, "fps": 1.0 / t,
         "cpu_baseline": {"value": value, "unit": "Mtris/s", "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -274,17 +298,23 @@ def measure_plain(sc, device, steps, warmup, flush_l2, workload=None, msaa_log2=
     ms = time_frames(r, stream, lambda: flush_l2(stream), lambda: r.RenderMesh(dm, synchronize=False),
                      steps, warmup) / steps
     st = r.Stats()
+    color, depth, tid = r.ReadOutputs()
     r.close()
     W, H = sc.view.width, sc.view.height
     return {"triangles": sc.mesh.nt, "width": W, "height": H, "ms_per_frame": ms,
             "mtris_per_s": sc.mesh.nt / ms / 1e3, "gpix_per_s": W * H / ms / 1e6, "fps": 1e3 / ms,
             "hbm_frac": algorithmic_bytes(sc) / (ms / 1e3) / 1e9 / load_peaks()[0],
-            "raster_triangles": int(st.raster_triangles), "bin_entries": int(st.bin_entries)}
+            "raster_triangles": int(st.raster_triangles), "bin_entries": int(st.bin_entries),
+            "parity": oracle_parity(sc.mesh, sc.view, color, depth, tid, msaa_log2=msaa_log2)}
 
 
-def measure_batched(device, steps, warmup, flush_l2):
-    """256 meshes x 4 orbit views at 512x512: one batched pass vs one plain pass per view."""
+def measure_batched(device, steps, warmup, flush_l2, oracle_views=16):
+    """256 meshes x 4 orbit views at 512x512: one batched pass against one
+    plain pass per view, and `oracle_views` batched views (spread from the
+    smallest mesh to the largest) against the CPU oracle."""
+    import ctypes
     import torch
+    from edxraster_gb300 import _lib
     from edxraster_gb300 import renderer as R
     meshes = scenes.batched_meshes(256, 500, 200_000, seed=11)
     views = []
@@ -300,44 +330,99 @@ def measure_batched(device, steps, warmup, flush_l2):
     batch = r.PrepareBatch(dms, views)
     ms_b = time_frames(r, stream, lambda: flush_l2(stream),
                        lambda: r.RenderBatched(batch, None, 512, 512, synchronize=False), steps, warmup) / steps
-    sample = list(range(0, len(views), 97))
+    by_size = sorted(range(len(views)), key=lambda i: (meshes[views[i].mesh].nt, i))
+    sample = sorted({by_size[round(k * (len(by_size) - 1) / (oracle_views - 1))] for k in range(oracle_views)})
     cb, db, tb = [], [], []
     for i in sample:
         c, d, t = r.ReadBatchOutputs(i, 1, 512, 512)
         cb.append(c[0])
         db.append(d[0])
         tb.append(t[0])
-    # one plain pass per view, in submission order
+    r.close()
+    checks = [oracle_parity(meshes[views[i].mesh], views[i], cb[j], db[j], tb[j]) for j, i in enumerate(sample)]
+    parity = {"views": len(sample), "triangles": [meshes[views[i].mesh].nt for i in sample],
+              "id_exact": all(c["id_exact"] for c in checks), "depth_exact": all(c["depth_exact"] for c in checks),
+              "color_err_max": max(c["color_err_max"] for c in checks)}
+
+    # One plain pass per view, in submission order.  The per-view arguments
+    # are built once (as PrepareBatch does for the batched pass), and each
+    # view is three calls of the C ABI: edxr_set_transform, edxr_set_shader,
+    # edxr_render.
     p = R.Renderer(device=device, stream=stream)
     p.Initialize(512, 512)
+    apply_tuning(p, "batched")
+    lib, h = p._lib, p._h
+    args = []
+    for v in views:
+        mv, pr, ra = R._f16(v.mv), R._f16(v.proj), R._f16(v.raster)
+        sp = _lib.ShaderParams((ctypes.c_float * 3)(*[float(x) for x in v.light]), v.ks, v.shininess)
+        args.append((mv, pr, ra, ctypes.addressof(mv), ctypes.addressof(pr), ctypes.addressof(ra), v.shader,
+                     ctypes.byref(sp), sp, ctypes.byref(batch[1][v.mesh])))
+    assert len({v.depth_func for v in views}) == 1
+    p.SetDepthFunc(views[0].depth_func)
 
-    def per_view():
-        for v in views:
-            R.configure(p, v)
-            p.RenderMesh(dms[v.mesh], synchronize=False)
+    def per_view(on_view=None):
+        for a in args:
+            _lib.check(lib.edxr_set_transform(h, a[3], a[4], a[5]))
+            _lib.check(lib.edxr_set_shader(h, 0, a[6], a[7]))
+            _lib.check(lib.edxr_render(h, a[9]))
+            if on_view:
+                on_view()
 
     per_view()
     p.Synchronize()
     torch.cuda.synchronize()
+    # (1) stream time: CUDA events around the whole loop on the renderer's
+    # stream (device time, including any gaps while the host issues views)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
+    e0.record(stream)
     per_view()
+    e1.record(stream)
     p.Synchronize()
     torch.cuda.synchronize()
-    ms_p = (time.perf_counter() - t0) * 1e3
+    ms_wall = (time.perf_counter() - t0) * 1e3
+    ms_stream = e0.elapsed_time(e1)
+    # (2) device time with the host ahead of the GPU: for each chunk of
+    # views the stream first runs a clock spin (torch.cuda._sleep) long
+    # enough for the host to queue the whole chunk behind it, and CUDA events
+    # bracket the chunk, whose passes then run back to back
+    chunk = 64
+    host_ms_per_view = ms_wall / len(args)
+    spin = int(4.0 * host_ms_per_view * chunk * 1e-3 * 2.07e9)  # cycles at the 2070 MHz maximum clock
+    ms_kernels = 0.0
+    for c0 in range(0, len(args), chunk):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            torch.cuda._sleep(spin)
+        e0.record(stream)
+        for a in args[c0:c0 + chunk]:
+            _lib.check(lib.edxr_set_transform(h, a[3], a[4], a[5]))
+            _lib.check(lib.edxr_set_shader(h, 0, a[6], a[7]))
+            _lib.check(lib.edxr_render(h, a[9]))
+        e1.record(stream)
+        p.Synchronize()
+        torch.cuda.synchronize()
+        ms_kernels += e0.elapsed_time(e1)
     exact = True
-    for j, i in enumerate(sample):
+    for j, i in enumerate(sample[:4]):
         R.configure(p, views[i])
         p.RenderMesh(dms[views[i].mesh])
         c, d, t = p.ReadOutputs()
         exact = exact and np.array_equal(t, tb[j]) and np.array_equal(d.view(np.uint32), db[j].view(np.uint32)) \
             and np.array_equal(c, cb[j])
     p.close()
-    r.close()
     tris = sum(meshes[v.mesh].nt for v in views)
     return {"views": len(views), "meshes": len(meshes), "triangles_per_pass": tris,
             "batched_ms": ms_b, "views_per_s": len(views) / ms_b * 1e3,
-            "plain_one_pass_per_view_ms": ms_p, "plain_views_per_s": len(views) / ms_p * 1e3,
-            "speedup_vs_plain": ms_p / ms_b, "bit_exact_sampled_views": exact, "sampled_views": len(sample)}
+            "plain_kernel_ms": ms_kernels, "plain_stream_ms": ms_stream, "plain_wall_ms": ms_wall,
+            "plain_views_per_s": len(views) / ms_kernels * 1e3,
+            "speedup_vs_plain": ms_kernels / ms_b,
+            "speedup_vs_plain_stream": ms_stream / ms_b, "speedup_vs_plain_wall": ms_wall / ms_b,
+            "speedup_basis": "device time against device time: the batched pass's CUDA-event time against the "
+                             "plain passes' CUDA-event time with the host queued ahead of the GPU (chunks of %d "
+                             "views behind a clock spin), so the plain passes run back to back" % chunk,
+            "bit_exact_vs_plain_views": exact, "parity": parity}
 
 
 def measure_diff(device, steps, warmup):
@@ -408,10 +493,18 @@ def measure_diff(device, steps, warmup):
 
     ms_f = timed(forward)
     ms_fb = timed(forward_backward)
+    r.RenderBatched(batch, None, 256, 256)
+    checks = []
+    for i in (0, n // 2, n - 1):
+        c, d, t = r.ReadBatchOutputs(i, 1, 256, 256)
+        checks.append(oracle_parity(mesh, views[i], c[0], d[0], t[0]))
     r.close()
+    parity = {"views": len(checks), "id_exact": all(c["id_exact"] for c in checks),
+              "depth_exact": all(c["depth_exact"] for c in checks),
+              "color_err_max": max(c["color_err_max"] for c in checks)}
     return {"triangles": mesh.nt, "views": n, "width": 256, "height": 256, "fwd_ms": ms_f,
             "fwd_iters_per_s": 1e3 / ms_f, "fwd_bwd_ms": ms_fb, "fwd_bwd_iters_per_s": 1e3 / ms_fb,
-            "fwd_bwd_over_fwd": ms_fb / ms_f}
+            "fwd_bwd_over_fwd": ms_fb / ms_f, "parity": parity}
 
 
 def measure_e2e(sc, device, steps, warmup, workload, world=1, renderers=E2E_RENDERERS):
@@ -537,6 +630,7 @@ def run_gpu(args, world, rank, local):
     achieved = raster_bytes / (raster_ms / 1e3) / 1e9
     frame_achieved = algorithmic_bytes(sc) / (ms_per_step / 1e3) / 1e9
 
+    frame_out = r.ReadOutputs()
     r.close()
     e2e = measure_e2e(sc, local, max(args.steps, E2E_MIN_FRAMES), args.warmup, args.workload, world)
 
@@ -563,14 +657,13 @@ def run_gpu(args, world, rank, local):
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(sc)
     traffic = traffic_from_profiles(args.workload)
+    parity = oracle_parity(sc.mesh, sc.view, *frame_out)
     line = {
         "metric": "Mtris/s", "value": value, "unit": "Mtris/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "ms_per_step_median": statistics.median(per),
         "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic (seeded scene generators)",
-        "config": {"workload": args.workload, "description": name, "triangles": sc.mesh.nt, "width": W,
-                   "height": H, "l2": "512 MiB write between timed frames",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(args.workload, sc, world),
         "gpix_per_s": world * W * H / (ms_per_step / 1e3) / 1e9,
         "fps": world * 1e3 / ms_per_step,
         "stage_ms": stage_ms,
@@ -585,6 +678,8 @@ def run_gpu(args, world, rank, local):
         "clocks": clock_info,
         "raster_triangles": int(stats.raster_triangles), "bin_entries": int(stats.bin_entries),
         "cpu_baseline": cpu,
+        "parity": parity,
+        "color_err_max": parity["color_err_max"],
         "per_config": per_config,
     }
     print(json.dumps(line), flush=True)

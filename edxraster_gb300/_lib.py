@@ -115,6 +115,7 @@ SIGNATURES = {
     "edxr_set_profiling": ([_P, ctypes.c_int], ctypes.c_int),
     "edxr_set_tuning": ([_P, ctypes.POINTER(Tuning)], ctypes.c_int),
     "edxr_get_tuning": ([_P, ctypes.POINTER(Tuning)], ctypes.c_int),
+    "edxr_debug_scan_stall": ([_P, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "edxr_get_stage_times": ([_P, _P, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
     "edxr_last_error_string": ([], ctypes.c_char_p),
     "edxr_render_batched": ([_P, ctypes.POINTER(Mesh), ctypes.c_uint32, ctypes.POINTER(View), ctypes.c_uint32,

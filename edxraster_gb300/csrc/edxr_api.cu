@@ -30,6 +30,115 @@ edxr_status fail(edxr_status s, const std::string& msg)
 
 void edxr::record_error(const char* msg) { g_last_error = msg; }
 
+void edxr::mat_mul(const float* A, const float* B, float* C)
+{
+    // P * MV as Renderer.cpp:90, each entry summed left to right in float
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
+        {
+            float s = A[i * 4] * B[j];
+            s = s + A[i * 4 + 1] * B[4 + j];
+            s = s + A[i * 4 + 2] * B[8 + j];
+            s = s + A[i * 4 + 3] * B[12 + j];
+            C[i * 4 + j] = s;
+        }
+}
+
+// Eye position MV^-1 * 0 (Renderer.cpp:289) by Gauss-Jordan in double.
+bool edxr::eye_from_mv(const float* mv, double eye[3])
+{
+    double a[4][8];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
+        {
+            a[i][j] = mv[i * 4 + j];
+            a[i][j + 4] = i == j ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 4; c++)
+    {
+        int piv = c;
+        for (int r = c + 1; r < 4; r++)
+            if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+        if (a[piv][c] == 0.0)
+            return false;
+        if (piv != c)
+            for (int j = 0; j < 8; j++) std::swap(a[c][j], a[piv][j]);
+        const double d = a[c][c];
+        for (int j = 0; j < 8; j++) a[c][j] /= d;
+        for (int r = 0; r < 4; r++)
+        {
+            if (r == c) continue;
+            const double m = a[r][c];
+            for (int j = 0; j < 8; j++) a[r][j] -= m * a[c][j];
+        }
+    }
+    const double w = a[3][7];
+    eye[0] = a[0][7] / w;
+    eye[1] = a[1][7] / w;
+    eye[2] = a[2][7] / w;
+    return true;
+}
+
+void edxr::frame_camera(FrameDesc& f, const float mv[16], const float proj[16], const float raster[16])
+{
+    mat_mul(proj, mv, f.mvp);
+    std::memcpy(f.raster, raster, sizeof(f.raster));
+    if (!eye_from_mv(mv, f.eye_d))
+        f.eye_d[0] = f.eye_d[1] = f.eye_d[2] = 0.0;
+    for (int q = 0; q < 3; q++)
+        f.eye[q] = (float)f.eye_d[q];
+    // 2D affine inverse of the raster matrix's x/y rows
+    const double a = raster[0], b = raster[1], c = raster[3];
+    const double d = raster[4], e = raster[5], g = raster[7];
+    const double det = a * e - b * d;
+    if (det != 0.0)
+    {
+        f.ndc_from_raster_d[0] = e / det;
+        f.ndc_from_raster_d[1] = -b / det;
+        f.ndc_from_raster_d[2] = (b * g - e * c) / det;
+        f.ndc_from_raster_d[3] = -d / det;
+        f.ndc_from_raster_d[4] = a / det;
+        f.ndc_from_raster_d[5] = (d * c - a * g) / det;
+        for (int q = 0; q < 6; q++)
+            f.ndc_from_raster[q] = (float)f.ndc_from_raster_d[q];
+    }
+}
+
+void edxr::frame_mesh(FrameDesc& f, const edxr_mesh& m, uint32_t width, uint32_t height)
+{
+    f.positions = static_cast<const char*>(m.positions);
+    f.normals = static_cast<const char*>(m.normals);
+    f.albedo = static_cast<const char*>(m.albedo);
+    f.uvs = static_cast<const char*>(m.uvs);
+    f.indices = m.indices;
+    f.pos_stride = m.position_stride;
+    f.nrm_stride = m.normal_stride;
+    f.alb_stride = m.albedo_stride;
+    f.uv_stride = m.uv_stride;
+    f.nv = m.num_vertices;
+    f.nt = m.num_triangles;
+    f.width = (int)width;
+    f.height = (int)height;
+    f.tdx = (int)((width + kTileSize - 1) >> kTileLog2);
+    f.tdy = (int)((height + kTileSize - 1) >> kTileLog2);
+    f.tdx32 = (int)((width + 31) >> 5);
+    f.tdy32 = (int)((height + 31) >> 5);
+}
+
+void edxr::frame_shading(FrameDesc& f, int ps_kind, const float light[3], float ks, float shininess)
+{
+    f.ps_kind = ps_kind;
+    for (int q = 0; q < 3; q++)
+        f.light_raw[q] = light[q];
+    const double lx = light[0], ly = light[1], lz = light[2];
+    const double ln = std::sqrt(lx * lx + ly * ly + lz * lz);
+    f.light[0] = (float)(lx / ln);
+    f.light[1] = (float)(ly / ln);
+    f.light[2] = (float)(lz / ln);
+    f.ks = ks;
+    f.shininess = shininess;
+}
+
 namespace {
 
 #define EDXR_CUDA(call)                                                                        \
@@ -77,55 +186,6 @@ struct DevBuf
     }
     template <typename T> T* as() const { return static_cast<T*>(ptr); }
 };
-
-void mat_mul(const float* A, const float* B, float* C)
-{
-    // P * MV as Renderer.cpp:90, each entry summed left to right in float
-    for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++)
-        {
-            float s = A[i * 4] * B[j];
-            s = s + A[i * 4 + 1] * B[4 + j];
-            s = s + A[i * 4 + 2] * B[8 + j];
-            s = s + A[i * 4 + 3] * B[12 + j];
-            C[i * 4 + j] = s;
-        }
-}
-
-// Eye position MV^-1 * 0 (Renderer.cpp:289) by Gauss-Jordan in double.
-bool eye_from_mv(const float* mv, double eye[3])
-{
-    double a[4][8];
-    for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++)
-        {
-            a[i][j] = mv[i * 4 + j];
-            a[i][j + 4] = i == j ? 1.0 : 0.0;
-        }
-    for (int c = 0; c < 4; c++)
-    {
-        int piv = c;
-        for (int r = c + 1; r < 4; r++)
-            if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
-        if (a[piv][c] == 0.0)
-            return false;
-        if (piv != c)
-            for (int j = 0; j < 8; j++) std::swap(a[c][j], a[piv][j]);
-        const double d = a[c][c];
-        for (int j = 0; j < 8; j++) a[c][j] /= d;
-        for (int r = 0; r < 4; r++)
-        {
-            if (r == c) continue;
-            const double m = a[r][c];
-            for (int j = 0; j < 8; j++) a[r][j] -= m * a[c][j];
-        }
-    }
-    const double w = a[3][7];
-    eye[0] = a[0][7] / w;
-    eye[1] = a[1][7] / w;
-    eye[2] = a[2][7] / w;
-    return true;
-}
 
 struct Camera
 {
@@ -356,57 +416,11 @@ void fill_frame(FrameDesc& f, const edxr_mesh& m, const Camera& cam, const Shadi
     f.texels = r->tex_texels.as<float4>();
     f.num_textures = r->num_textures;
     f.tex_filter = r->state.texture_filter;
-    f.positions = static_cast<const char*>(m.positions);
-    f.normals = static_cast<const char*>(m.normals);
-    f.albedo = static_cast<const char*>(m.albedo);
-    f.uvs = static_cast<const char*>(m.uvs);
-    f.indices = m.indices;
-    f.pos_stride = m.position_stride;
-    f.nrm_stride = m.normal_stride;
-    f.alb_stride = m.albedo_stride;
-    f.uv_stride = m.uv_stride;
-    f.nv = m.num_vertices;
-    f.nt = m.num_triangles;
-    f.width = (int)width;
-    f.height = (int)height;
-    f.tdx = (int)((width + kTileSize - 1) >> kTileLog2);
-    f.tdy = (int)((height + kTileSize - 1) >> kTileLog2);
-    f.tdx32 = (int)((width + 31) >> 5);
-    f.tdy32 = (int)((height + 31) >> 5);
-    f.ps_kind = sh.ps_kind;
+    frame_mesh(f, m, width, height);
     f.depth_func = depth_func;
     f.hierarchical = hierarchical ? 1 : 0;
-    mat_mul(cam.proj, cam.mv, f.mvp);
-    std::memcpy(f.raster, cam.raster, sizeof(f.raster));
-    if (!eye_from_mv(cam.mv, f.eye_d))
-        f.eye_d[0] = f.eye_d[1] = f.eye_d[2] = 0.0;
-    for (int q = 0; q < 3; q++)
-    {
-        f.eye[q] = (float)f.eye_d[q];
-        f.light_raw[q] = sh.p.light[q];
-    }
-    const double lx = sh.p.light[0], ly = sh.p.light[1], lz = sh.p.light[2];
-    const double ln = std::sqrt(lx * lx + ly * ly + lz * lz);
-    f.light[0] = (float)(lx / ln);
-    f.light[1] = (float)(ly / ln);
-    f.light[2] = (float)(lz / ln);
-    f.ks = sh.p.ks;
-    f.shininess = sh.p.shininess;
-    // 2D affine inverse of the raster matrix's x/y rows
-    const double a = cam.raster[0], b = cam.raster[1], c = cam.raster[3];
-    const double d = cam.raster[4], e = cam.raster[5], g = cam.raster[7];
-    const double det = a * e - b * d;
-    if (det != 0.0)
-    {
-        f.ndc_from_raster_d[0] = e / det;
-        f.ndc_from_raster_d[1] = -b / det;
-        f.ndc_from_raster_d[2] = (b * g - e * c) / det;
-        f.ndc_from_raster_d[3] = -d / det;
-        f.ndc_from_raster_d[4] = a / det;
-        f.ndc_from_raster_d[5] = (d * c - a * g) / det;
-        for (int q = 0; q < 6; q++)
-            f.ndc_from_raster[q] = (float)f.ndc_from_raster_d[q];
-    }
+    frame_camera(f, cam.mv, cam.proj, cam.raster);
+    frame_shading(f, sh.ps_kind, sh.p.light, sh.p.ks, sh.p.shininess);
 }
 
 // Build the pass over `n` frames (already in r->frames_host) and launch it,
@@ -984,6 +998,21 @@ edxr_status edxr_set_tuning(edxr_renderer* r, const edxr_tuning* t)
     r->tuning.bin_blocks_per_sm = t->bin_blocks_per_sm;
     r->tuning.raster_blocks_per_sm = t->raster_blocks_per_sm;
     r->bins_per_tri = t->bin_entries_per_triangle;
+    return EDXR_OK;
+}
+
+edxr_status edxr_debug_scan_stall(edxr_renderer* r, int block, int spin_limit)
+{
+    if (!r)
+        return fail(EDXR_ERR_INVALID_ARG, "NULL renderer");
+    if (block < -1 || spin_limit < 0)
+        return fail(EDXR_ERR_INVALID_ARG, "scan stall block must be >= -1 and the spin limit >= 0");
+    DeviceGuard g(r->device);
+    edxr_status s = sync_pass(r);
+    if (s != EDXR_OK)
+        return s;
+    r->tuning.scan_stall_block = block;
+    r->tuning.scan_spin_limit = spin_limit;
     return EDXR_OK;
 }
 

@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "edxr.h"
+
 namespace edxr {
 
 // 16x16-pixel bin tiles.  Each is exactly one quadrant of a 32x32 tile of the
@@ -139,6 +141,11 @@ struct Tuning
     int raster_variant;   // 0/1: k_raster with the triangle-parallel path (uncapped / 5 blocks), 2: pixel-parallel only
     int bin_blocks_per_sm;
     int raster_blocks_per_sm;  // 0 = as many as fit
+    // Failure test of the scan's bounded wait (edxr_debug_scan_stall): scan
+    // block scan_stall_block (-1: none) does not publish its sum, and a wait
+    // gives up after scan_spin_limit polls (0: kScanSpinLimit).
+    int scan_stall_block;
+    int scan_spin_limit;
 };
 
 // Launch parameters shared by every kernel of one pass.
@@ -196,6 +203,18 @@ Tuning default_tuning();
 // Sets the message edxr_last_error_string returns on this thread.
 void record_error(const char* msg);
 void prepare_kernels();
+// Host-side fill of a frame descriptor, shared by every entry point so that
+// all of them hand the kernels identical frames (edxr_api.cu).
+// C = A * B of row-major 4x4 matrices, each entry summed left to right in float.
+void mat_mul(const float* A, const float* B, float* C);
+// Object-space eye position MV^-1 * 0 in double; false if MV is singular.
+bool eye_from_mv(const float* mv, double eye[3]);
+// Mesh pointers, strides, counts and the framebuffer's tile grids.
+void frame_mesh(FrameDesc& f, const edxr_mesh& m, uint32_t width, uint32_t height);
+// MVP = proj * mv, the raster matrix, the eye position and the raster-to-NDC inverse.
+void frame_camera(FrameDesc& f, const float mv[16], const float proj[16], const float raster[16]);
+// Pixel shader kind, normalised and raw light direction, ks and shininess.
+void frame_shading(FrameDesc& f, int ps_kind, const float light[3], float ks, float shininess);
 cudaError_t launch_back_buffer(const float4* color, uint8_t* rgba8, int width, int height, cudaStream_t s);
 // One mip level: each texel the mean of the 2x2 texels above it (indices
 // clamped to the source size).

@@ -708,6 +708,10 @@ __global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
     // the filled parts of the stripes (slots past a stripe's end were
     // dropped: overflow), numbered one after another
     __shared__ uint32_t s_first[kBinStripes + 1];
+    // a pass that reported an error (a scan wait that ran out, a bad index)
+    // fails as a whole: its offsets may be wrong, so nothing is scattered
+    if (*(volatile uint32_t*)&a.status->error)
+        return;
     const uint64_t R = stripe_slots(a.bin_capacity);
     const uint32_t lane = threadIdx.x & 31;
     if (threadIdx.x < 32)
@@ -989,18 +993,25 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
     if (threadIdx.x == 0)
     {
         uint32_t prefix = 0;
+        // (a failure test makes one block keep its sums to itself)
+        const bool publish = (int)b != a.tune.scan_stall_block;
+        const int spin_limit = a.tune.scan_spin_limit > 0 ? a.tune.scan_spin_limit : kScanSpinLimit;
         if (b == 0)
-            atomicExch(&a.scan_status[0], kScanPrefix | total);
+        {
+            if (publish)
+                atomicExch(&a.scan_status[0], kScanPrefix | total);
+        }
         else
         {
-            atomicExch(&a.scan_status[b], kScanAggregate | total);
+            if (publish)
+                atomicExch(&a.scan_status[b], kScanAggregate | total);
             for (int j = (int)b - 1; j >= 0;)
             {
                 unsigned long long st = 0;
                 int spins = 0;
                 do
                     st = *(volatile unsigned long long*)&a.scan_status[j];
-                while (st == 0 && ++spins < kScanSpinLimit);
+                while (st == 0 && ++spins < spin_limit);
                 if (st == 0)
                 {
                     // a range never published: report it, never hang
@@ -1012,7 +1023,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
                     break;
                 j--;
             }
-            atomicExch(&a.scan_status[b], kScanPrefix | (prefix + total));
+            if (publish)
+                atomicExch(&a.scan_status[b], kScanPrefix | (prefix + total));
         }
         s_prefix = prefix;
     }
@@ -1365,6 +1377,8 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
 {
     __shared__ unsigned long long s_key[kRasterWarps][256];
     __shared__ StagedSlot s_tri[kRasterWarps][32];
+    if (*(volatile uint32_t*)&a.status->error)
+        return;  // the pass failed (see k_bin_move); every thread of the block leaves
     // ceil(65536 / w): ((p * s_recip[w]) >> 16) == p / w for 0 <= p < 256 and
     // 1 <= w <= 16, the row of pixel p of a region w pixels wide
     __shared__ uint32_t s_recip[17];
@@ -1691,6 +1705,8 @@ template <int S>
 __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
 {
     extern __shared__ unsigned long long ms_shared[];
+    if (*(volatile uint32_t*)&a.status->error)
+        return;  // the pass failed (see k_bin_move); every thread of the block leaves
     // ceil(65536 / w): ((p * s_recip[w]) >> 16) == p / w for 0 <= p < 256
     // and 1 <= w <= 16, the row of pixel p of a region w pixels wide
     __shared__ uint32_t s_recip[17];
@@ -1961,6 +1977,8 @@ Tuning default_tuning()
     t.raster_variant = 1;
     t.bin_blocks_per_sm = 8;
     t.raster_blocks_per_sm = 0;
+    t.scan_stall_block = -1;
+    t.scan_spin_limit = 0;
     return t;
 }
 

@@ -24,7 +24,9 @@
 //  * Sizes beyond the fixed limits below are rejected with
 //    EDXR_ERR_INVALID_ARG before any GPU work; a frame whose bins do not fit
 //    fails with EDXR_ERR_OVERFLOW (nothing can grow).
-//  * The call waits for its frame on `stream` before returning.
+//  * Every call blocks the calling thread: it copies the frame descriptor
+//    from its own stack, then waits on `stream` for the frame and reads the
+//    status word back before returning.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -111,50 +113,6 @@ edxr_status scratch_for_device(int device, unsigned char** base, int* sms)
     return EDXR_OK;
 }
 
-void mat_mul_rm(const float* A, const float* B, float* C)
-{
-    for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++)
-        {
-            float s = A[i * 4] * B[j];
-            s = s + A[i * 4 + 1] * B[4 + j];
-            s = s + A[i * 4 + 2] * B[8 + j];
-            s = s + A[i * 4 + 3] * B[12 + j];
-            C[i * 4 + j] = s;
-        }
-}
-
-bool eye_position(const float* mv, double eye[3])
-{
-    double a[4][8];
-    for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++)
-        {
-            a[i][j] = mv[i * 4 + j];
-            a[i][j + 4] = i == j ? 1.0 : 0.0;
-        }
-    for (int c = 0; c < 4; c++)
-    {
-        int piv = c;
-        for (int r = c + 1; r < 4; r++)
-            if (fabs(a[r][c]) > fabs(a[piv][c])) piv = r;
-        if (a[piv][c] == 0.0)
-            return false;
-        if (piv != c)
-            for (int j = 0; j < 8; j++) { const double t = a[c][j]; a[c][j] = a[piv][j]; a[piv][j] = t; }
-        const double d = a[c][c];
-        for (int j = 0; j < 8; j++) a[c][j] /= d;
-        for (int r = 0; r < 4; r++)
-        {
-            if (r == c) continue;
-            const double m = a[r][c];
-            for (int j = 0; j < 8; j++) a[r][j] -= m * a[c][j];
-        }
-    }
-    for (int q = 0; q < 3; q++) eye[q] = a[q][7] / a[3][7];
-    return true;
-}
-
 }  // namespace
 
 extern "C" {
@@ -207,38 +165,11 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
 
     FrameDesc f;
     memset(&f, 0, sizeof(f));
-    f.positions = static_cast<const char*>(mesh->positions);
-    f.normals = static_cast<const char*>(mesh->normals);
-    f.albedo = static_cast<const char*>(mesh->albedo);
-    f.uvs = static_cast<const char*>(mesh->uvs);
-    f.indices = mesh->indices;
-    f.pos_stride = mesh->position_stride;
-    f.nrm_stride = mesh->normal_stride;
-    f.alb_stride = mesh->albedo_stride;
-    f.uv_stride = mesh->uv_stride;
-    f.nv = mesh->num_vertices;
-    f.nt = mesh->num_triangles;
-    f.width = (int)width;
-    f.height = (int)height;
-    f.tdx = (int)((width + kTileSize - 1) >> kTileLog2);
-    f.tdy = (int)((height + kTileSize - 1) >> kTileLog2);
-    f.tdx32 = (int)((width + 31) >> 5);
-    f.tdy32 = (int)((height + 31) >> 5);
-    f.ps_kind = ps_kind;
+    frame_mesh(f, *mesh, width, height);
     f.depth_func = state->depth_func;
     f.hierarchical = state->hierarchical ? 1 : 0;
-    mat_mul_rm(proj, mv, f.mvp);
-    memcpy(f.raster, raster, sizeof(f.raster));
-    if (!eye_position(mv, f.eye_d))
-        f.eye_d[0] = f.eye_d[1] = f.eye_d[2] = 0.0;
-    for (int q = 0; q < 3; q++)
-    {
-        f.eye[q] = (float)f.eye_d[q];
-        f.light[q] = (float)(params->light[q] / ln);
-        f.light_raw[q] = params->light[q];
-    }
-    f.ks = params->ks;
-    f.shininess = params->shininess;
+    frame_camera(f, mv, proj, raster);
+    frame_shading(f, ps_kind, params->light, params->ks, params->shininess);
     const uint32_t tiles = (uint32_t)(f.tdx * f.tdy);
 
     PassArgs a;
@@ -288,7 +219,9 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
         cudaStreamSynchronize(s) != cudaSuccess)
         return noalloc_fail(EDXR_ERR_CUDA, "frame execution failed");
     if (ds.error)
-        return noalloc_fail(EDXR_ERR_INVALID_ARG, "a triangle references a vertex index out of range");
+        return noalloc_fail((edxr_status)ds.error, ds.error == EDXR_ERR_INVALID_ARG
+                                                       ? "a triangle references a vertex index out of range"
+                                                       : "the device reported an error (a bounded wait ran out)");
     if (ds.overflow)
         return noalloc_fail(EDXR_ERR_OVERFLOW, "the frame needs more bins or clipped polygons than the fixed scratch holds");
     return EDXR_OK;

@@ -301,6 +301,15 @@ typedef struct edxr_tuning
 edxr_status edxr_set_tuning(edxr_renderer* r, const edxr_tuning* tuning);
 edxr_status edxr_get_tuning(edxr_renderer* r, edxr_tuning* tuning);
 
+/* Failure test of the binning scan's bounded wait; no counterpart in the
+ * reference, whose binning has no wait and no overflow check (Tile.h:34).
+ * Block `block` of the tile-count scan (blocks of 1024 tiles in launch
+ * order; -1 = none, the default) keeps its sums to itself, so the block
+ * after it waits `spin_limit` polls (0 = the default limit, about a second)
+ * and gives up: the frame fails with EDXR_ERR_TIMEOUT instead of hanging,
+ * and the renderer stays usable. */
+edxr_status edxr_debug_scan_stall(edxr_renderer* r, int block, int spin_limit);
+
 /* Message of the last failing call on this thread. */
 const char* edxr_last_error_string(void);
 
@@ -384,11 +393,13 @@ edxr_status edxr_backward(edxr_renderer* r, const edxr_mesh* mesh, const edxr_sh
  * loads the library until exit); nothing is allocated.  Limits: 65536
  * vertices, 65536 triangles, 4096 pixels per side and 2^20 pixels; larger
  * requests fail with EDXR_ERR_INVALID_ARG, and a frame whose bins or clipped
- * polygons do not fit fails with EDXR_ERR_OVERFLOW.  The first call on a
- * device looks the array up with cudaGetSymbolAddress: make it before any
- * stream capture.  Calls share the array and keep its contents; calls whose
- * GPU work overlaps race, so serialise them.  The call waits for the frame
- * on `stream` (a cudaStream_t, NULL = legacy default stream). */
+ * polygons do not fit fails with EDXR_ERR_OVERFLOW (the array cannot grow,
+ * so the frame is not rendered again; the next call renders normally).  The
+ * first call on a device looks the array up with cudaGetSymbolAddress: make
+ * it before any stream capture.  Calls share the array and keep its
+ * contents; calls whose GPU work overlaps race, so serialise them.  Every
+ * call blocks the calling thread until its frame on `stream` (a cudaStream_t,
+ * NULL = legacy default stream) has finished and its status is read back. */
 edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const float proj[16],
                                 const float raster[16], const edxr_state* state, int ps_kind,
                                 const edxr_shader_params* params, uint32_t width, uint32_t height,

@@ -8,8 +8,8 @@
   where they lie (``EDXRaster/Core/Renderer.cpp``, ``FrameBuffer.cpp``,
   ``Scene.cpp`` and the headers they include), against the project-written
   EDXUtil shim in ``oracle/shim`` plus ``oracle/ref_harness.cpp``, into
-  ``oracle/_ref/libedxr_ref.so``.  It needs the reference checkout
-  (``EDXR_REFERENCE_ROOT``, default ``/root/reference``); without it the
+  ``oracle/_ref/libedxr_ref.so``.  It needs the reference checkout: ``EDXR_REFERENCE_ROOT``, else a
+  ``reference`` directory beside the repository's own; without it the
   reference build is skipped and only the restatement exists.
 
 Run ``python -m oracle.build`` to build both.
@@ -27,7 +27,8 @@ REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "libedxr_oracle.so")
 REF_SO = os.path.join(REF_DIR, "libedxr_ref.so")
 
-REFERENCE_ROOT = os.environ.get("EDXR_REFERENCE_ROOT", "/root/reference")
+REFERENCE_ROOT = os.environ.get("EDXR_REFERENCE_ROOT",
+                                os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 FLAGS = ["-O2", "-fPIC", "-fwrapv", "-ffp-contract=off"]
 
 

@@ -49,6 +49,7 @@ def test_null_renderer_is_rejected(cuda_lib):
     assert cuda_lib.edxr_resize(None, 64, 64) == INVALID
     assert cuda_lib.edxr_synchronize(None) == INVALID
     assert cuda_lib.edxr_set_shader(None, 0, 0, None) == INVALID
+    assert cuda_lib.edxr_debug_scan_stall(None, 0, 16) == INVALID
 
 
 def _noalloc_case(**change):

@@ -106,3 +106,31 @@ def test_depth_funcs_on_coplanar_layers(cuda_lib):
     for f in (scenes.DEPTH_LEQUAL, scenes.DEPTH_LESS):
         sc.view.depth_func = f
         assert_parity(sc)
+
+
+def test_scan_wait_runs_out_and_renderer_recovers(cuda_lib):
+    """The tile-count scan's bounded wait: a scan block that never publishes
+    its sum (edxr_debug_scan_stall) makes the next block give up after a short
+    spin limit.  The frame fails with EDXR_ERR_TIMEOUT instead of hanging, the
+    kernels after the scan do nothing, and the next frame on the same renderer
+    is exact.  (The reference's binning has neither a wait nor a check,
+    Tile.h:34.)"""
+    from edxraster_gb300 import _lib
+    sc = scenes.terrain_scene(96, 640, 480, seed=3)  # 40 x 30 = 1,200 tiles: two scan blocks
+    r = R.Renderer()
+    r.Initialize(sc.view.width, sc.view.height)
+    R.configure(r, sc.view)
+    dm = R.DeviceMesh.from_mesh(sc.mesh)
+    _lib.check(r._lib.edxr_debug_scan_stall(r._h, 0, 4096))
+    with pytest.raises(_lib.EdxrError) as err:
+        r.RenderMesh(dm)
+    assert err.value.status == 3  # EDXR_ERR_TIMEOUT
+    _lib.check(r._lib.edxr_debug_scan_stall(r._h, -1, 0))
+    r.RenderMesh(dm)
+    c, d, t = r.ReadOutputs()
+    r.close()
+    o = pyoracle.render_oracle(sc.mesh, sc.view)
+    assert not mismatch_report("triangle id", t, o["id"])
+    assert not mismatch_report("depth", d.view(np.uint32), o["depth"].view(np.uint32))
+    cov = t != 0xFFFFFFFF
+    assert cov.any() and float(np.abs(c[cov, :3] - o["color"][cov, :3]).max()) <= 1e-5

@@ -36,7 +36,8 @@ def render_regular(sc):
     return out
 
 
-def render_noalloc(lib, sc, stream):
+def call_noalloc(lib, sc, stream):
+    """One edxr_render_noalloc call; returns its status and the three images."""
     import torch
     v = sc.view
     dm = R.DeviceMesh.from_mesh(sc.mesh)
@@ -48,12 +49,37 @@ def render_noalloc(lib, sc, stream):
     params = _lib.ShaderParams((ctypes.c_float * 3)(*[float(x) for x in v.light]), v.ks, v.shininess)
     mesh = dm.abi()
     mv, proj, raster = _f16(v.mv), _f16(v.proj), _f16(v.raster)
-    _lib.check(lib.edxr_render_noalloc(ctypes.byref(mesh), ctypes.addressof(mv), ctypes.addressof(proj),
-                                       ctypes.addressof(raster), ctypes.byref(state), v.shader, ctypes.byref(params),
-                                       W, H, color.data_ptr(), depth.data_ptr(), tid.data_ptr(),
-                                       stream.cuda_stream))
+    rc = lib.edxr_render_noalloc(ctypes.byref(mesh), ctypes.addressof(mv), ctypes.addressof(proj),
+                                 ctypes.addressof(raster), ctypes.byref(state), v.shader, ctypes.byref(params),
+                                 W, H, color.data_ptr(), depth.data_ptr(), tid.data_ptr(), stream.cuda_stream)
     torch.cuda.synchronize()
-    return color.cpu().numpy(), depth.cpu().numpy(), tid.cpu().numpy().view(np.uint32)
+    return rc, (color.cpu().numpy(), depth.cpu().numpy(), tid.cpu().numpy().view(np.uint32))
+
+
+def render_noalloc(lib, sc, stream):
+    rc, out = call_noalloc(lib, sc, stream)
+    _lib.check(rc)
+    return out
+
+
+def left_edge_scene(n=12000, width=256, height=256, seed=5):
+    """n triangles that each straddle the left clip plane (x = -w): every one
+    is queued for clipping, more than the 8192 clipped polygons the fixed
+    array holds."""
+    rng = np.random.default_rng(seed)
+    y = rng.uniform(-0.8, 0.8, size=n)
+    w = rng.uniform(1.0, 2.0, size=n)
+    ndc = np.stack([np.stack([np.full(n, -1.4), y], -1), np.stack([np.full(n, -0.9), y + 0.05], -1),
+                    np.stack([np.full(n, -0.9), y - 0.05], -1)], 1)  # (n, 3, 2)
+    pos = np.concatenate([ndc * w[:, None, None], np.repeat(w[:, None, None], 3, 1)], -1).reshape(-1, 3)
+    nrm = np.tile(np.array([0.0, 0.0, -1.0], np.float32), (3 * n, 1))
+    mesh = scenes.Mesh(pos.astype(np.float32), nrm, np.full((3 * n, 3), 0.5, np.float32),
+                       np.zeros((3 * n, 2), np.float32), np.arange(3 * n, dtype=np.uint32).reshape(n, 3))
+    proj = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, scenes.STRESS_A, scenes.STRESS_B], [0, 0, 1, 0]],
+                    np.float32)
+    view = scenes.View(width, height, np.eye(4, dtype=np.float32), proj, scenes.raster_matrix(width, height),
+                       np.array([0.3, 0.5, -1.0], np.float32))
+    return scenes.Scene("left_edge", mesh, view)
 
 
 def test_noalloc_matches_render_twice(cuda_lib):
@@ -86,3 +112,21 @@ def test_noalloc_rejects_sizes_over_its_limits(cuda_lib):
                                       64, 64, out.data_ptr(), out.data_ptr(), out.data_ptr(), None)
     assert rc == 1  # EDXR_ERR_INVALID_ARG
     assert b"limit" in cuda_lib.edxr_last_error_string()
+
+
+def test_noalloc_overflow_then_next_frame_exact(cuda_lib):
+    """A frame that does not fit the fixed array fails with EDXR_ERR_OVERFLOW
+    (it cannot grow and render again, as edxr_render does); the next call on
+    the same array, which the failed frame left behind, renders exactly."""
+    import torch
+    stream = torch.cuda.Stream()
+    rc, _ = call_noalloc(cuda_lib, left_edge_scene(), stream)
+    assert rc == 2  # EDXR_ERR_OVERFLOW
+    assert b"scratch" in cuda_lib.edxr_last_error_string()
+    sc = scenes.stress_scene(20000, 640, 360, seed=9, max_area=3e3)
+    c0, d0, t0 = render_regular(sc)
+    c1, d1, t1 = render_noalloc(cuda_lib, sc, stream)
+    assert np.array_equal(t1, t0)
+    assert np.array_equal(d1.view(np.uint32), d0.view(np.uint32))
+    assert (t0 != 0xFFFFFFFF).any()
+    assert float(np.abs(c1 - c0).max()) <= COLOR_TOL
