@@ -383,27 +383,15 @@ def measure_batched(device, steps, warmup, flush_l2, oracle_views=16):
     torch.cuda.synchronize()
     ms_wall = (time.perf_counter() - t0) * 1e3
     ms_stream = e0.elapsed_time(e1)
-    # (2) device time with the host ahead of the GPU: for each chunk of
-    # views the stream first runs a clock spin (torch.cuda._sleep) long
-    # enough for the host to queue the whole chunk behind it, and CUDA events
-    # bracket the chunk, whose passes then run back to back
-    chunk = 64
-    host_ms_per_view = ms_wall / len(args)
-    spin = int(4.0 * host_ms_per_view * chunk * 1e-3 * 2.07e9)  # cycles at the 2070 MHz maximum clock
-    ms_kernels = 0.0
-    for c0 in range(0, len(args), chunk):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            torch.cuda._sleep(spin)
-        e0.record(stream)
-        for a in args[c0:c0 + chunk]:
-            _lib.check(lib.edxr_set_transform(h, a[3], a[4], a[5]))
-            _lib.check(lib.edxr_set_shader(h, 0, a[6], a[7]))
-            _lib.check(lib.edxr_render(h, a[9]))
-        e1.record(stream)
-        p.Synchronize()
-        torch.cuda.synchronize()
-        ms_kernels += e0.elapsed_time(e1)
+    # (2) device time of each plain pass, from before its first kernel to
+    # after its last (stage events), summed over the views.  A plain pass
+    # waits for the previous frame's status word (its overflow check) before
+    # it is issued, so the passes of different views cannot overlap.
+    p.SetProfiling(True)
+    acc = [0.0]
+    per_view(lambda: acc.__setitem__(0, acc[0] + sum(p.StageTimes().values())))
+    p.SetProfiling(False)
+    ms_kernels = acc[0]
     exact = True
     for j, i in enumerate(sample[:4]):
         R.configure(p, views[i])
@@ -420,8 +408,8 @@ def measure_batched(device, steps, warmup, flush_l2, oracle_views=16):
             "speedup_vs_plain": ms_kernels / ms_b,
             "speedup_vs_plain_stream": ms_stream / ms_b, "speedup_vs_plain_wall": ms_wall / ms_b,
             "speedup_basis": "device time against device time: the batched pass's CUDA-event time against the "
-                             "plain passes' CUDA-event time with the host queued ahead of the GPU (chunks of %d "
-                             "views behind a clock spin), so the plain passes run back to back" % chunk,
+                             "sum over views of each plain pass's CUDA-event time from its first kernel to its "
+                             "last (stage events)",
             "bit_exact_vs_plain_views": exact, "parity": parity}
 
 
