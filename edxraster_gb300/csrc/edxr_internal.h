@@ -138,7 +138,7 @@ struct DeviceStatus
 struct Tuning
 {
     int small_region;     // bin entries whose pixel region is at most this are rasterized triangle-parallel
-    int raster_variant;   // 0/1: k_raster with the triangle-parallel path (uncapped / 5 blocks), 2: pixel-parallel only
+    int raster_variant;   // 0/1: k_raster with the triangle-parallel path (3 / 5 blocks per SM), 2: pixel-parallel only
     int bin_blocks_per_sm;
     int raster_blocks_per_sm;  // 0 = as many as fit
     // Failure test of the scan's bounded wait (edxr_debug_scan_stall): scan

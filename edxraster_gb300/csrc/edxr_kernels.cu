@@ -1333,6 +1333,15 @@ __device__ __forceinline__ uint32_t raster_triangle_of(const PassArgs& a, uint32
     return ri < nr ? ri : kNoTriangle;
 }
 
+// *p -= v at device scope with acquire-release semantics; returns the old
+// value.  A split tile's items count its entries down with it (see k_raster).
+__device__ __forceinline__ uint32_t atomic_sub_acq_rel(uint32_t* p, uint32_t v)
+{
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;\n" : "=r"(old) : "l"(p), "r"(0u - v) : "memory");
+    return old;
+}
+
 // The one write of a pixel (Renderer::FragmentProcessing / UpdateFrameBuffer,
 // Renderer.cpp:272-350, shade every fragment and keep the last; only the
 // winner is shaded here): its barycentrics and depth are recomputed exactly
@@ -1534,15 +1543,17 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
                 if (px < f.width && py < f.height && kk < clear)
                     atomicMax(&a.keybuf[f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px], ~kk);
             }
-            __threadfence();
+            // The countdown is one acquire-release atomic: the lanes' merges
+            // happen before it (warp barrier, then lane 0's release), and
+            // the item that counts the tile down to zero acquires every
+            // other item's merges before it reads them back.
             __syncwarp();
             uint32_t left = 0;
             if (lane == 0)
-                left = atomicSub(&a.tile_cursor[tile], e1 - e0) - (e1 - e0);
+                left = atomic_sub_acq_rel(&a.tile_cursor[tile], e1 - e0) - (e1 - e0);
             shade = __shfl_sync(0xffffffffu, left, 0) == 0;
             if (shade)
             {
-                __threadfence();
 #pragma unroll
                 for (int k = 0; k < 8; k++)
                 {
@@ -1833,15 +1844,14 @@ __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
                 if (px < f.width && py < f.height && kk < clear)
                     atomicMax(&a.keybuf[s * plane + f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px], ~kk);
             }
-            __threadfence();
+            // acquire-release countdown, as in k_raster
             __syncwarp();
             uint32_t left = 0;
             if (lane == 0)
-                left = atomicSub(&a.tile_cursor[tile], e1 - e0) - (e1 - e0);
+                left = atomic_sub_acq_rel(&a.tile_cursor[tile], e1 - e0) - (e1 - e0);
             shade = __shfl_sync(0xffffffffu, left, 0) == 0;
             if (shade)
             {
-                __threadfence();
                 for (int k = (int)lane; k < 256 * S; k += 32)
                 {
                     const int s = k >> 8, p = k & 255;
@@ -1900,8 +1910,9 @@ __global__ void k_back_buffer(const float4* color, uchar4* out, int width, int h
 
 // -------------------------------------------------------------------------
 
-// Raster variants: 0 and 1 carry the triangle-parallel path (no register cap /
-// capped for 5 blocks per SM); 2 is pixel-parallel only, capped for 6.
+// Raster variants: 0 and 1 carry the triangle-parallel path (3 blocks per SM,
+// whose 85 registers a thread hold the shading epilogue without spills / 5
+// blocks per SM); 2 is pixel-parallel only, capped for 6.
 static int raster_occupancy(int variant)
 {
     static int per_sm[3] = { 0, 0, 0 };
@@ -1909,7 +1920,7 @@ static int raster_occupancy(int variant)
     {
         cudaError_t e;
         if (variant == 0)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[0], k_raster<4, true>, kRasterThreads, 0);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[0], k_raster<3, true>, kRasterThreads, 0);
         else if (variant == 1)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[1], k_raster<5, true>, kRasterThreads, 0);
         else
@@ -2022,7 +2033,7 @@ cudaError_t launch_pipeline(const PassArgs& a, cudaStream_t s, cudaEvent_t* ev)
     else if (a.tune.raster_variant == 1)
         k_raster<5, true><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
     else
-        k_raster<4, true><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
+        k_raster<3, true><<<raster_blocks(sms, a.tune), kRasterThreads, 0, s>>>(a);
     mark(5);
     return cudaGetLastError();
 }

@@ -290,7 +290,8 @@ typedef struct edxr_tuning
 {
     int small_region;             /* bin entries whose pixel region in a 16x16 tile is at most this
                                      many pixels are rasterized one triangle per thread; 0 disables */
-    int raster_variant;           /* 0: raster kernel with the triangle-parallel path, no register cap;
+    int raster_variant;           /* 0: raster kernel with the triangle-parallel path, 3 blocks per SM
+                                        (85 registers a thread, no spills);
                                      1: the same capped for 5 blocks per SM;
                                      2: pixel-parallel only (small_region ignored), capped for 6 */
     int bin_blocks_per_sm;        /* grid of the per-triangle binning kernels */
