@@ -676,6 +676,25 @@ def run_gpu(args, world, rank, local):
     return 0
 
 
+def profile_frames(args):
+    """Frames of the workload for a profiler (ncu): device-resident mesh, one
+    synchronised RenderMesh per frame, no timing and no JSON line."""
+    import torch
+    from edxraster_gb300 import renderer as R
+    sc = WORKLOADS[args.workload][1]()
+    r = R.Renderer(device=0)
+    r.Initialize(sc.view.width, sc.view.height)
+    R.configure(r, sc.view)
+    apply_tuning(r, args.workload)
+    dm = R.DeviceMesh.from_mesh(sc.mesh, device="cuda:0")
+    for _ in range(args.profile_frames):
+        r.RenderMesh(dm)
+    torch.cuda.synchronize()
+    r.close()
+    print("rendered %d frames of %s" % (args.profile_frames, args.workload))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -685,7 +704,11 @@ def main():
     ap.add_argument("--workload", default="terrain", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the per-configuration measurements")
+    ap.add_argument("--profile-frames", type=int, default=0,
+                    help="render this many frames of the workload and exit (a target for a profiler; no timing)")
     args = ap.parse_args()
+    if args.profile_frames:
+        return profile_frames(args)
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_setup()

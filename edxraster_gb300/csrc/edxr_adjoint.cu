@@ -60,6 +60,51 @@ __device__ __forceinline__ V3 ld(const char* base, uint32_t stride, uint32_t i, 
 // gradient of normalize(x) applied to dy: (dy - y (y . dy)) / |x|
 __device__ __forceinline__ V3 normalize_grad(V3 y, float lenx, V3 dy) { return (1.0f / lenx) * (dy - dot(y, dy) * y); }
 
+// Float pairs: the value hi + lo, |lo| <= ulp(hi) / 2.
+struct FF
+{
+    float hi, lo;
+};
+// a * b exactly, as a pair (needs the product rounded once: the library is
+// built without contraction, and fmaf gives the exact remainder).
+__device__ __forceinline__ FF two_prod(float a, float b)
+{
+    const float p = a * b;
+    return { p, fmaf(a, b, -p) };
+}
+// a + b exactly, as a pair.
+__device__ __forceinline__ FF two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float bb = s - a;
+    return { s, (a - (s - bb)) + (b - bb) };
+}
+__device__ __forceinline__ FF quick_two_sum(float a, float b)  // |a| >= |b|
+{
+    const float s = a + b;
+    return { s, b - (s - a) };
+}
+__device__ __forceinline__ FF ff_add(FF x, FF y)
+{
+    const FF s = two_sum(x.hi, y.hi);
+    return quick_two_sum(s.hi, s.lo + (x.lo + y.lo));
+}
+__device__ __forceinline__ FF ff_sub(FF x, FF y) { return ff_add(x, { -y.hi, -y.lo }); }
+__device__ __forceinline__ FF ff_mul(FF x, FF y)
+{
+    const FF p = two_prod(x.hi, y.hi);
+    return quick_two_sum(p.hi, p.lo + (x.hi * y.lo + x.lo * y.hi));
+}
+__device__ __forceinline__ FF ff_mul_f(FF x, float y)
+{
+    const FF p = two_prod(x.hi, y);
+    return quick_two_sum(p.hi, p.lo + x.lo * y);
+}
+// m0 x + m1 y + m2 z + m3 as a pair.
+__device__ __forceinline__ FF ff_dot4(float m0, float m1, float m2, float m3, float x, float y, float z)
+{
+    return ff_add(ff_add(two_prod(m0, x), two_prod(m1, y)), ff_add(two_prod(m2, z), { m3, 0.0f }));
+}
 // Everything the forward computes for one pixel, kept for the adjoint.
 struct PixelState
 {
@@ -86,48 +131,56 @@ __device__ __forceinline__ bool pixel_forward(const FrameDesc& f, const DiffMesh
         s.n[k] = ld(m.normals, m.nrm_stride, s.vi[k], 0.0f);
         s.a[k] = ld(m.albedo, m.alb_stride, s.vi[k], 1.0f);
     }
-    // The solve cancels heavily (a_k, c_k are the small projected distances of
-    // the vertices from the pixel centre, each a difference of O(1) terms), so
-    // the clip coordinates, the pixel centre and the solve run in FP64; the
-    // result is rounded to float once.  FP64 is the slow unit of this GPU:
-    // the products are fused explicitly (fma) and S is inverted once.
-    double X[3], Y[3], Wd[3], ac[3], cc[3], bt[3];
+    // The solve cancels heavily: a_k, c_k are the small projected distances of
+    // the vertices from the pixel centre, each a difference of O(1) terms.
+    // The clip coordinates and the pixel centre are therefore carried as
+    // float pairs (hi + lo, about 48 bits; error-free products and sums,
+    // Dekker 1971 / Knuth), and so are a_k, c_k, the cross products and their
+    // sum, each rounded to float once: FP32 arithmetic throughout, accurate
+    // to a few float ulps of the results, without the FP64 unit (slow on
+    // this GPU).
     const float* M = f.mvp;
+    FF X[3], Y[3], Wd[3];
     for (int k = 0; k < 3; k++)
     {
-        const double x = s.p[k].x, y = s.p[k].y, z = s.p[k].z;
-        X[k] = fma((double)M[0], x, fma((double)M[1], y, fma((double)M[2], z, (double)M[3])));
-        Y[k] = fma((double)M[4], x, fma((double)M[5], y, fma((double)M[6], z, (double)M[7])));
-        Wd[k] = fma((double)M[12], x, fma((double)M[13], y, fma((double)M[14], z, (double)M[15])));
-        s.X[k] = (float)X[k];
-        s.Y[k] = (float)Y[k];
-        s.W[k] = (float)Wd[k];
+        const float x = s.p[k].x, y = s.p[k].y, z = s.p[k].z;
+        X[k] = ff_dot4(M[0], M[1], M[2], M[3], x, y, z);
+        Y[k] = ff_dot4(M[4], M[5], M[6], M[7], x, y, z);
+        Wd[k] = ff_dot4(M[12], M[13], M[14], M[15], x, y, z);
+        s.X[k] = X[k].hi + X[k].lo;
+        s.Y[k] = Y[k].hi + Y[k].lo;
+        s.W[k] = Wd[k].hi + Wd[k].lo;
     }
-    const double rx = (double)px + 0.5, ry = (double)py + 0.5;
-    const double* R = f.ndc_from_raster_d;
-    const double u = fma(R[0], rx, fma(R[1], ry, R[2]));
-    const double v = fma(R[3], rx, fma(R[4], ry, R[5]));
-    s.u = (float)u;
-    s.v = (float)v;
+    const float rx = (float)px + 0.5f, ry = (float)py + 0.5f;  // exact
+    const float* Rh = f.ndc_from_raster;
+    const float* Rl = f.ndc_from_raster_lo;
+    const FF u = ff_add(ff_add(ff_mul_f({ Rh[0], Rl[0] }, rx), ff_mul_f({ Rh[1], Rl[1] }, ry)), { Rh[2], Rl[2] });
+    const FF v = ff_add(ff_add(ff_mul_f({ Rh[3], Rl[3] }, rx), ff_mul_f({ Rh[4], Rl[4] }, ry)), { Rh[5], Rl[5] });
+    s.u = u.hi + u.lo;
+    s.v = v.hi + v.lo;
+    FF ac[3], cc[3];
     for (int k = 0; k < 3; k++)
     {
-        ac[k] = fma(-u, Wd[k], X[k]);
-        cc[k] = fma(-v, Wd[k], Y[k]);
-        s.ac[k] = (float)ac[k];
-        s.cc[k] = (float)cc[k];
+        ac[k] = ff_sub(X[k], ff_mul(u, Wd[k]));
+        cc[k] = ff_sub(Y[k], ff_mul(v, Wd[k]));
+        s.ac[k] = ac[k].hi + ac[k].lo;
+        s.cc[k] = cc[k].hi + cc[k].lo;
     }
-    bt[0] = fma(ac[1], cc[2], -(ac[2] * cc[1]));
-    bt[1] = fma(ac[2], cc[0], -(ac[0] * cc[2]));
-    bt[2] = fma(ac[0], cc[1], -(ac[1] * cc[0]));
-    const double S = bt[0] + bt[1] + bt[2];
-    if (!(S != 0.0))
+    // the cross products and their sum stay pairs too: near an edge, or on a
+    // thin triangle, they cancel again
+    FF bt[3];
+    bt[0] = ff_sub(ff_mul(ac[1], cc[2]), ff_mul(ac[2], cc[1]));
+    bt[1] = ff_sub(ff_mul(ac[2], cc[0]), ff_mul(ac[0], cc[2]));
+    bt[2] = ff_sub(ff_mul(ac[0], cc[1]), ff_mul(ac[1], cc[0]));
+    const FF Sf = ff_add(ff_add(bt[0], bt[1]), bt[2]);
+    const float S = Sf.hi + Sf.lo;
+    if (!(S != 0.0f) || !(fabsf(S) < 3.0e38f))
         return false;
-    s.S = (float)S;
-    const double invS = 1.0 / S;
+    s.S = S;
     for (int k = 0; k < 3; k++)
     {
-        s.bt[k] = (float)bt[k];
-        s.b[k] = (float)(bt[k] * invS);
+        s.bt[k] = bt[k].hi + bt[k].lo;
+        s.b[k] = s.bt[k] / S;
     }
     s.P = s.b[0] * s.p[0] + s.b[1] * s.p[1] + s.b[2] * s.p[2];
     s.Nraw = s.b[0] * s.n[0] + s.b[1] * s.n[1] + s.b[2] * s.n[2];

@@ -100,7 +100,10 @@ void edxr::frame_camera(FrameDesc& f, const float mv[16], const float proj[16], 
         f.ndc_from_raster_d[4] = a / det;
         f.ndc_from_raster_d[5] = (d * c - a * g) / det;
         for (int q = 0; q < 6; q++)
+        {
             f.ndc_from_raster[q] = (float)f.ndc_from_raster_d[q];
+            f.ndc_from_raster_lo[q] = (float)(f.ndc_from_raster_d[q] - (double)f.ndc_from_raster[q]);
+        }
     }
 }
 

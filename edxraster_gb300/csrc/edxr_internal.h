@@ -90,6 +90,8 @@ struct FrameDesc
     float pad2;
     double eye_d[3];           // eye position in double (FP64 shading)
     double ndc_from_raster_d[6];  // the raster-to-NDC inverse in double (differentiable form)
+    float ndc_from_raster_lo[6];  // ndc_from_raster_d - ndc_from_raster: with it, a float pair (hi + lo)
+    float pad3[2];
     // textures of the textured Lambertian shader
     const uint32_t* tex_ids;      // per input triangle (NULL: slot 0)
     const TexDesc* textures;
