@@ -671,9 +671,12 @@ __device__ __forceinline__ float3 persp_bary(const RTri& t, int px, int py)
 // pixel's 2x2 quad (LambertianAlbedoPixelShader, Shader.h:226-228: lane 1
 // minus lane 0 and lane 2 minus lane 0, the quad's top-left pixel being
 // lane 0), all from t's perspective-correct barycentrics.
-__device__ __forceinline__ float3 texture_albedo(const FrameDesc& f, const RTri& t, const ClipPoly* polys, int px,
-                                                 int py)
+// (Out of line, and handed the record's address in global memory, so that a
+// caller's copy of it can stay in registers.)
+static __device__ __noinline__ float3 texture_albedo(const FrameDesc& f, const RTri* tg, const ClipPoly* polys, int px,
+                                                    int py)
 {
+    const RTri t = *tg;
     const uint32_t tri = t.order >> 4;
     const uint32_t slot = f.tex_ids ? __ldg(f.tex_ids + tri) : 0u;
     if (slot >= f.num_textures || !f.uvs)
@@ -723,9 +726,10 @@ __device__ __forceinline__ float3 texture_albedo(const FrameDesc& f, const RTri&
 // the error of N.H by ks*s*x^(s-1) = 600: FP32 unit vectors cannot hold N.H
 // to the ~5e-9 that 1e-5 of colour needs, so this shader interpolates and
 // shades in FP64.
-static __device__ __noinline__ float3 shade_fragment_fp64(const FrameDesc& f, const RTri& t, const ClipPoly* polys,
+static __device__ __noinline__ float3 shade_fragment_fp64(const FrameDesc& f, const RTri* tg, const ClipPoly* polys,
                                                    float l0, float l1)
 {
+    const RTri t = *tg;
     double b0 = l0, b1 = l1;
     double b2 = 1.0 - b0 - b1;
     b0 *= (double)t.invW0;
@@ -764,11 +768,12 @@ static __device__ __noinline__ float3 shade_fragment_fp64(const FrameDesc& f, co
 
 // Fragment::Interpolate (Shader.h:142-170) from the fragment's barycentrics,
 // then the shading model.
-__device__ __forceinline__ float3 shade_fragment(const FrameDesc& f, const RTri& t, const ClipPoly* polys,
-                                                 float l0, float l1, int px, int py)
+// t is the record at tg (global memory).
+__device__ __forceinline__ float3 shade_fragment(const FrameDesc& f, const RTri& t, const RTri* tg,
+                                                 const ClipPoly* polys, float l0, float l1, int px, int py)
 {
     if (f.ps_kind == 1)
-        return shade_fragment_fp64(f, t, polys, l0, l1);
+        return shade_fragment_fp64(f, tg, polys, l0, l1);
     float b0 = l0, b1 = l1;
     float b2 = fsub(fsub(1.0f, b0), b1);
     b0 = fmul(b0, t.invW0);
@@ -781,7 +786,7 @@ __device__ __forceinline__ float3 shade_fragment(const FrameDesc& f, const RTri&
     const ShadeVerts v = shade_verts(f, t, polys);
     const float3 P = lerp3(b0, v.p[0], b1, v.p[1], b2, v.p[2]);
     const float3 N = lerp3(b0, v.n[0], b1, v.n[1], b2, v.n[2]);
-    const float3 A = f.ps_kind == 4 ? texture_albedo(f, t, polys, px, py) : lerp3(b0, v.a[0], b1, v.a[1], b2, v.a[2]);
+    const float3 A = f.ps_kind == 4 ? texture_albedo(f, tg, polys, px, py) : lerp3(b0, v.a[0], b1, v.a[1], b2, v.a[2]);
     return shade_model(f, P, N, A);
 }
 

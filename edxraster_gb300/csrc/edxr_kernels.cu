@@ -1375,7 +1375,7 @@ static __device__ __forceinline__ void write_pixel(const PixelOut a, const Frame
     const float L1 = fmul(__int2float_rn(n2), t.invDet);
     const float L2 = fsub(fsub(1.0f, L0), L1);
     const float d = fadd(fadd(fmul(L0, t.z0), fmul(L1, t.z1)), fmul(L2, t.z2));
-    const float3 c = shade_fragment(f, t, a.polys, L0, L1, px, py);
+    const float3 c = shade_fragment(f, t, a.rtris + ri, a.polys, L0, L1, px, py);
     a.color[pix] = make_float4(c.x, c.y, c.z, 1.0f);
     a.depth[pix] = d;
     a.tri_id[pix] = t.order >> 4;
@@ -1687,7 +1687,7 @@ static __device__ __forceinline__ void write_pixel_ms(const PassArgs& a, const F
             t = a.rtris[r];
             float L0, L1;
             depth_at(t, (px << 4) + 8, (py << 4) + 8, L0, L1);
-            const float3 c = shade_fragment(f, t, a.polys, L0, L1, px, py);
+            const float3 c = shade_fragment(f, t, a.rtris + r, a.polys, L0, L1, px, py);
             cf[0] = fdiv((float)to_byte(c.x), 255.0f);
             cf[1] = fdiv((float)to_byte(c.y), 255.0f);
             cf[2] = fdiv((float)to_byte(c.z), 255.0f);
