@@ -1342,6 +1342,19 @@ __device__ __forceinline__ uint32_t atomic_sub_acq_rel(uint32_t* p, uint32_t v)
     return old;
 }
 
+// Depth of raster triangle t at 1/16-pixel position (x, y)
+// (RasterTriangle.h:324-337).
+__device__ __forceinline__ float depth_at(const RTri& t, int x, int y, float& L0, float& L1)
+{
+    const Edges e = tri_edges(t);
+    const int n1 = wadd(wmul(e.B[1], wsub(x, t.v2x)), wmul(e.C[1], wsub(y, t.v2y)));
+    const int n2 = wadd(wmul(e.B[2], wsub(x, t.v2x)), wmul(e.C[2], wsub(y, t.v2y)));
+    L0 = fmul(__int2float_rn(n1), t.invDet);
+    L1 = fmul(__int2float_rn(n2), t.invDet);
+    const float L2 = fsub(fsub(1.0f, L0), L1);
+    return fadd(fadd(fmul(L0, t.z0), fmul(L1, t.z1)), fmul(L2, t.z2));
+}
+
 // The one write of a pixel (Renderer::FragmentProcessing / UpdateFrameBuffer,
 // Renderer.cpp:272-350, shade every fragment and keep the last; only the
 // winner is shaded here): its barycentrics and depth are recomputed exactly
@@ -1379,6 +1392,68 @@ static __device__ __forceinline__ void write_pixel(const PixelOut a, const Frame
     a.color[pix] = make_float4(c.x, c.y, c.z, 1.0f);
     a.depth[pix] = d;
     a.tri_id[pix] = t.order >> 4;
+}
+
+// The per-vertex-attribute shaders (Blinn-Phong, Lambertian with or without
+// albedo): no call inside.
+static __device__ __forceinline__ void write_pixel_fast(const PixelOut a, const FrameDesc& f, uint32_t ri,
+                                                        uint64_t pix, int px, int py)
+{
+    if (ri == kNoTriangle)
+    {
+        a.color[pix] = make_float4(0.f, 0.f, 0.f, 0.f);
+        a.depth[pix] = 1.0f;
+        a.tri_id[pix] = kNoTriangle;
+        return;
+    }
+    const RTri t = a.rtris[ri];
+    float L0, L1;
+    const float d = depth_at(t, (px << 4) + 8, (py << 4) + 8, L0, L1);
+    float b0 = L0, b1 = L1;
+    float b2 = fsub(fsub(1.0f, b0), b1);
+    b0 = fmul(b0, t.invW0);
+    b1 = fmul(b1, t.invW1);
+    b2 = fmul(b2, t.invW2);
+    const float invB = __frcp_rn(fadd(fadd(b0, b1), b2));
+    b0 = fmul(b0, invB);
+    b1 = fmul(b1, invB);
+    b2 = fsub(fsub(1.0f, b0), b1);
+    const ShadeVerts v = shade_verts(f, t, a.polys);
+    const float3 c = shade_model(f, lerp3(b0, v.p[0], b1, v.p[1], b2, v.p[2]), lerp3(b0, v.n[0], b1, v.n[1], b2, v.n[2]),
+                                 lerp3(b0, v.a[0], b1, v.a[1], b2, v.a[2]));
+    a.color[pix] = make_float4(c.x, c.y, c.z, 1.0f);
+    a.depth[pix] = d;
+    a.tri_id[pix] = t.order >> 4;
+}
+
+// A tile shaded by the FP64 or the textured shader: out of line, pixel by
+// pixel, so that the common shaders' loop keeps its registers.
+static __device__ __noinline__ void shade_tile_slow(const PixelOut out, const FrameDesc& f,
+                                                    const unsigned long long* key, int tileX, int tileY, bool less,
+                                                    uint32_t nr, const uint32_t* tri_first, uint32_t total_tris)
+{
+    const uint32_t lane = threadIdx.x & 31;
+#pragma unroll 1
+    for (int k = 0; k < 8; k++)
+    {
+        const int p = (int)lane + 32 * k;
+        const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
+        if (px >= f.width || py >= f.height)
+            continue;
+        const uint32_t low = (uint32_t)key[p];
+        const uint32_t rank = less ? low : ~low;
+        uint32_t ri = kNoTriangle;
+        if (rank)
+        {
+            // raster_triangle_of on the pass's tables
+            const uint32_t gi = (rank - 1u) >> 4, fan = (rank - 1u) & 15u;
+            if (gi < total_tris)
+                ri = fan == 0 ? gi : tri_first[gi] + fan - 1u;
+            if (ri >= nr)
+                ri = kNoTriangle;
+        }
+        write_pixel(out, f, ri, f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px, px, py);
+    }
 }
 
 template <int MinBlocks, bool SmallPath>
@@ -1569,7 +1644,9 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
                 }
             }
         }
-        if (shade)
+        if (shade && (f.ps_kind == 1 || f.ps_kind == 4))
+            shade_tile_slow(out, f, key, tileX, tileY, less, nr, a.tri_first, a.total_tris);
+        else if (shade)
         {
 #pragma unroll 1
             for (int k = 0; k < 8; k++)
@@ -1579,7 +1656,7 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
                 const uint32_t low = (uint32_t)key[p];
                 const uint32_t ri = raster_triangle_of(a, less ? low : ~low, nr);
                 if (px < f.width && py < f.height)
-                    write_pixel(out, f, ri, f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px, px, py);
+                    write_pixel_fast(out, f, ri, f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px, px, py);
             }
         }
         __syncwarp();
@@ -1645,18 +1722,6 @@ __device__ __forceinline__ uint32_t to_byte(float v)
     return (uint32_t)fadd(fmul(v, 255.0f), 0.5f);
 }
 
-// Depth of raster triangle t at 1/16-pixel position (x, y)
-// (RasterTriangle.h:324-337).
-__device__ __forceinline__ float depth_at(const RTri& t, int x, int y, float& L0, float& L1)
-{
-    const Edges e = tri_edges(t);
-    const int n1 = wadd(wmul(e.B[1], wsub(x, t.v2x)), wmul(e.C[1], wsub(y, t.v2y)));
-    const int n2 = wadd(wmul(e.B[2], wsub(x, t.v2x)), wmul(e.C[2], wsub(y, t.v2y)));
-    L0 = fmul(__int2float_rn(n1), t.invDet);
-    L1 = fmul(__int2float_rn(n2), t.invDet);
-    const float L2 = fsub(fsub(1.0f, L0), L1);
-    return fadd(fadd(fmul(L0, t.z0), fmul(L1, t.z1)), fmul(L2, t.z2));
-}
 
 // The output of one pixel with S samples: per sample the winner's id and its
 // depth at the sample; the colour is the reference's resolve
