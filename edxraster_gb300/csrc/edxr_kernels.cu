@@ -24,7 +24,7 @@ constexpr int kRasterThreads = 256;    // 8 warps, each on its own work items
 constexpr uint32_t kBigChunk = 128;    // unsorted-list slots a k_bin_big warp reserves at a time
 constexpr uint32_t kEmptySlot = 0xFFFFFFFFu;
 constexpr uint32_t kSplitTile = 0x80000000u;  // item tag: the tile has several items (tiles < 2^24)
-constexpr uint32_t kHeavyItem = 64;    // raster items with this many entries are handed out first
+constexpr uint32_t kHeavyItem = 96;    // raster items with this many entries are handed out first
 
 // Clip-space position of vertex v: clip = MVP * (p, 1) (DefaultVertexShader,
 // Shader.h:40-49).
@@ -1627,6 +1627,7 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
             if (lane == 0)
                 left = atomic_sub_acq_rel(&a.tile_cursor[tile], e1 - e0) - (e1 - e0);
             shade = __shfl_sync(0xffffffffu, left, 0) == 0;
+            __syncwarp();  // lane 0's acquire, then every lane's reads
             if (shade)
             {
 #pragma unroll
@@ -1915,6 +1916,7 @@ __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
             if (lane == 0)
                 left = atomic_sub_acq_rel(&a.tile_cursor[tile], e1 - e0) - (e1 - e0);
             shade = __shfl_sync(0xffffffffu, left, 0) == 0;
+            __syncwarp();  // lane 0's acquire, then every lane's reads
             if (shade)
             {
                 for (int k = (int)lane; k < 256 * S; k += 32)
