@@ -54,7 +54,7 @@ WORKLOADS = {
                lambda: scenes.stress_scene(1_000_000, 3840, 2160, seed=7)),
 }
 PIXEL_BYTES = 24  # RGBA32F colour + D32F depth + u32 triangle id per pixel
-E2E_RENDERERS = 4  # frames in flight in the end-to-end measurement
+E2E_RENDERERS = 6  # frames in flight in the end-to-end measurement
 E2E_MIN_FRAMES = 64  # end-to-end frames timed at least (each renderer's thread start is in the timed region)
 
 

@@ -15,8 +15,7 @@
 //  * The array is part of the library image: every GPU that loads the library
 //    holds kNoAllocScratchBytes of it until the process exits.
 //  * The first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current); make that first call
-//    before any stream capture on the device.
+//    cudaGetSymbolAddress (with that device current).
 //  * Every call on a device shares the one array and leaves its contents
 //    behind; the pass clears what must start at zero itself.  Calls whose GPU
 //    work overlaps (several host threads, or several streams) race on the

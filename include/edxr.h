@@ -396,9 +396,9 @@ edxr_status edxr_backward(edxr_renderer* r, const edxr_mesh* mesh, const edxr_sh
  * requests fail with EDXR_ERR_INVALID_ARG, and a frame whose bins or clipped
  * polygons do not fit fails with EDXR_ERR_OVERFLOW (the array cannot grow,
  * so the frame is not rendered again; the next call renders normally).  The
- * first call on a device looks the array up with cudaGetSymbolAddress: make
- * it before any stream capture.  Calls share the array and keep its
- * contents; calls whose GPU work overlaps race, so serialise them.  Every
+ * first call on a device looks the array up with cudaGetSymbolAddress.
+ * Calls share the array and keep its contents; calls whose GPU work
+ * overlaps race, so serialise them.  Every
  * call blocks the calling thread until its frame on `stream` (a cudaStream_t,
  * NULL = legacy default stream) has finished and its status is read back. */
 edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const float proj[16],
