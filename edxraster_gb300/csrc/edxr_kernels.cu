@@ -1395,7 +1395,27 @@ static __device__ __forceinline__ void write_pixel(const PixelOut a, const Frame
 }
 
 // The per-vertex-attribute shaders (Blinn-Phong, Lambertian with or without
-// albedo): no call inside.
+// albedo) at barycentrics (L0, L1) of raster triangle t: perspective-correct
+// weights, the vertices' attributes, the shading model.  No call inside.
+static __device__ __forceinline__ float3 shade_common(const FrameDesc& f, const RTri& t, const ClipPoly* polys,
+                                                      float L0, float L1)
+{
+    float b0 = L0, b1 = L1;
+    float b2 = fsub(fsub(1.0f, b0), b1);
+    b0 = fmul(b0, t.invW0);
+    b1 = fmul(b1, t.invW1);
+    b2 = fmul(b2, t.invW2);
+    const float invB = __frcp_rn(fadd(fadd(b0, b1), b2));
+    b0 = fmul(b0, invB);
+    b1 = fmul(b1, invB);
+    b2 = fsub(fsub(1.0f, b0), b1);
+    const ShadeVerts v = shade_verts(f, t, polys);
+    return shade_model(f, lerp3(b0, v.p[0], b1, v.p[1], b2, v.p[2]), lerp3(b0, v.n[0], b1, v.n[1], b2, v.n[2]),
+                       lerp3(b0, v.a[0], b1, v.a[1], b2, v.a[2]));
+}
+
+// The one write of a pixel for the per-vertex-attribute shaders: no call
+// inside.
 static __device__ __forceinline__ void write_pixel_fast(const PixelOut a, const FrameDesc& f, uint32_t ri,
                                                         uint64_t pix, int px, int py)
 {
@@ -1409,18 +1429,7 @@ static __device__ __forceinline__ void write_pixel_fast(const PixelOut a, const 
     const RTri t = a.rtris[ri];
     float L0, L1;
     const float d = depth_at(t, (px << 4) + 8, (py << 4) + 8, L0, L1);
-    float b0 = L0, b1 = L1;
-    float b2 = fsub(fsub(1.0f, b0), b1);
-    b0 = fmul(b0, t.invW0);
-    b1 = fmul(b1, t.invW1);
-    b2 = fmul(b2, t.invW2);
-    const float invB = __frcp_rn(fadd(fadd(b0, b1), b2));
-    b0 = fmul(b0, invB);
-    b1 = fmul(b1, invB);
-    b2 = fsub(fsub(1.0f, b0), b1);
-    const ShadeVerts v = shade_verts(f, t, a.polys);
-    const float3 c = shade_model(f, lerp3(b0, v.p[0], b1, v.p[1], b2, v.p[2]), lerp3(b0, v.n[0], b1, v.n[1], b2, v.n[2]),
-                                 lerp3(b0, v.a[0], b1, v.a[1], b2, v.a[2]));
+    const float3 c = shade_common(f, t, a.polys, L0, L1);
     a.color[pix] = make_float4(c.x, c.y, c.z, 1.0f);
     a.depth[pix] = d;
     a.tri_id[pix] = t.order >> 4;
@@ -1730,7 +1739,12 @@ __device__ __forceinline__ uint32_t to_byte(float v)
 // winner's colour shaded at the pixel centre as 8 bits (Renderer.cpp:
 // 295-350), the samples are averaged in float (alpha 1 per covered sample,
 // 0 for the clear value).  Samples that share a winner share its shading.
-static __device__ __forceinline__ void write_pixel_ms(const PassArgs& a, const FrameDesc& f, const uint32_t* ri, int S,
+// The winners come from the pixel's keys (key[s * 256], shared memory), read
+// sample by sample.  Common: the per-vertex-attribute shaders, inline (no
+// call); otherwise shade_fragment (the FP64 and textured shaders out of line).
+template <bool Common>
+static __device__ __forceinline__ void write_pixel_ms(const PassArgs& a, const FrameDesc& f,
+                                                   const unsigned long long* key, bool less, uint32_t nr, int S,
                                                    uint64_t pix, int px, int py)
 {
     const int level = a.msaa_log2;
@@ -1741,7 +1755,8 @@ static __device__ __forceinline__ void write_pixel_ms(const PassArgs& a, const F
     RTri t;                            // the record of `last`
     for (int s = 0; s < S; s++)
     {
-        const uint32_t r = ri[s];
+        const uint32_t low = (uint32_t)key[s * 256];
+        const uint32_t r = raster_triangle_of(a, less ? low : ~low, nr);
         if (r == kNoTriangle)
         {
             a.depth[s * plane + pix] = 1.0f;
@@ -1753,7 +1768,8 @@ static __device__ __forceinline__ void write_pixel_ms(const PassArgs& a, const F
             t = a.rtris[r];
             float L0, L1;
             depth_at(t, (px << 4) + 8, (py << 4) + 8, L0, L1);
-            const float3 c = shade_fragment(f, t, a.rtris + r, a.polys, L0, L1, px, py);
+            const float3 c = Common ? shade_common(f, t, a.polys, L0, L1)
+                                    : shade_fragment(f, t, a.rtris + r, a.polys, L0, L1, px, py);
             cf[0] = fdiv((float)to_byte(c.x), 255.0f);
             cf[1] = fdiv((float)to_byte(c.y), 255.0f);
             cf[2] = fdiv((float)to_byte(c.z), 255.0f);
@@ -1772,14 +1788,37 @@ static __device__ __forceinline__ void write_pixel_ms(const PassArgs& a, const F
     a.color[pix] = make_float4(fmul(acc[0], inv), fmul(acc[1], inv), fmul(acc[2], inv), fmul(acc[3], inv));
 }
 
+// A multisampled tile shaded by the FP64 or the textured shader: out of line,
+// so that the common shaders' loop keeps its registers.  (`a` is the
+// kernel's grid-constant parameter: passed by address, it is not copied.)
+static __device__ __noinline__ void shade_tile_ms_slow(const PassArgs& a, const FrameDesc& f,
+                                                       const unsigned long long* key, int tileX, int tileY, bool less,
+                                                       uint32_t nr, int S)
+{
+    const uint32_t lane = threadIdx.x & 31;
+#pragma unroll 1
+    for (int k = 0; k < 8; k++)
+    {
+        const int p = (int)lane + 32 * k;
+        const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
+        if (px >= f.width || py >= f.height)
+            continue;
+        write_pixel_ms<false>(a, f, key + p, less, nr, S, f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px,
+                              px, py);
+    }
+}
+
 // Raster with S samples per pixel: persistent warps on the same work items
 // as k_raster, keys [sample][pixel] in dynamic shared memory, every entry's
 // (entry, pixel) pairs spread over the lanes with a loop over the samples,
 // entries behind the tile's samples skipped.  Split tiles merge per sample
 // in the key buffer (S planes).
 
+// Blocks of 4 warps (2 with 16 samples, 1 with 32); registers capped where
+// shared memory lets 5 blocks share an SM (2 and 4 samples: 96 registers a
+// thread), the compiler's choice where it lets 3.
 template <int S>
-__global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
+__global__ void __launch_bounds__(128, S <= 4 ? 5 : 3) k_raster_ms(const __grid_constant__ PassArgs a)
 {
     extern __shared__ unsigned long long ms_shared[];
     if (*(volatile uint32_t*)&a.status->error)
@@ -1933,7 +1972,9 @@ __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
                 __syncwarp();
             }
         }
-        if (shade)
+        if (shade && (f.ps_kind == 1 || f.ps_kind == 4))
+            shade_tile_ms_slow(a, f, key, tileX, tileY, less, nr, S);
+        else if (shade)
         {
 #pragma unroll 1
             for (int k = 0; k < 8; k++)
@@ -1942,14 +1983,8 @@ __global__ void __launch_bounds__(128) k_raster_ms(PassArgs a)
                 const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
                 if (px >= f.width || py >= f.height)
                     continue;
-                uint32_t ri[S];
-#pragma unroll
-                for (int s = 0; s < S; s++)
-                {
-                    const uint32_t low = (uint32_t)key[s * 256 + p];
-                    ri[s] = raster_triangle_of(a, less ? low : ~low, nr);
-                }
-                write_pixel_ms(a, f, ri, S, f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px, px, py);
+                write_pixel_ms<true>(a, f, key + p, less, nr, S,
+                                     f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px, px, py);
             }
         }
         __syncwarp();
