@@ -686,12 +686,14 @@ def profile_frames(args):
     r.Initialize(sc.view.width, sc.view.height)
     R.configure(r, sc.view)
     apply_tuning(r, args.workload)
+    if args.msaa:
+        r.SetMSAAMode(args.msaa)
     dm = R.DeviceMesh.from_mesh(sc.mesh, device="cuda:0")
     for _ in range(args.profile_frames):
         r.RenderMesh(dm)
     torch.cuda.synchronize()
     r.close()
-    print("rendered %d frames of %s" % (args.profile_frames, args.workload))
+    print("rendered %d frames of %s (%d samples per pixel)" % (args.profile_frames, args.workload, 1 << args.msaa))
     return 0
 
 
@@ -706,6 +708,8 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the per-configuration measurements")
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="render this many frames of the workload and exit (a target for a profiler; no timing)")
+    ap.add_argument("--msaa", type=int, default=0, choices=range(0, 6),
+                    help="with --profile-frames: 2^MSAA samples per pixel")
     args = ap.parse_args()
     if args.profile_frames:
         return profile_frames(args)
