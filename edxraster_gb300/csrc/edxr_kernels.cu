@@ -1704,25 +1704,21 @@ __device__ __forceinline__ int sample_offset(int level, int s) { return kSampleO
 __device__ __forceinline__ bool sample_key(const StagedTri& st, const int* G, int lx, int ly, int o, bool less,
                                            uint64_t& key)
 {
+    // (no early exit: lanes of a warp test different samples, and the
+    // arithmetic of an uncovered one costs the warp nothing extra)
     const uint32_t fl = st.flags;
     const int l1 = wadd(wadd(wadd(wmul(st.A1, lx), wmul(st.D1, ly)), st.K1), wmul(o, G[1]));
     const int l2 = wadd(wadd(wadd(wmul(st.A2, lx), wmul(st.D2, ly)), st.K2), wmul(o, G[2]));
-    if (!(fl & (1u << 20)))
-    {
-        const int e0 = wadd(wadd(wadd(wmul(st.A0, lx), wmul(st.D0, ly)), st.K0), wmul(o, G[0]));
-        const int e1 = wadd(l1, (fl & (1u << 21)) ? -1 : 0);
-        const int e2 = wadd(l2, (fl & (1u << 22)) ? -1 : 0);
-        if ((e0 | e1 | e2) < 0)
-            return false;
-    }
+    const int e0 = wadd(wadd(wadd(wmul(st.A0, lx), wmul(st.D0, ly)), st.K0), wmul(o, G[0]));
+    const int e1 = wadd(l1, (fl & (1u << 21)) ? -1 : 0);
+    const int e2 = wadd(l2, (fl & (1u << 22)) ? -1 : 0);
+    const bool inside = (fl & (1u << 20)) || (e0 | e1 | e2) >= 0;
     const float L0 = fmul(__int2float_rn(l1), st.invDet);
     const float L1 = fmul(__int2float_rn(l2), st.invDet);
     const float L2 = fsub(fsub(1.0f, L0), L1);
     const float d = fadd(fadd(fmul(L0, st.z0), fmul(L1, st.z1)), fmul(L2, st.z2));
-    if (d != d)
-        return false;
     key = ((uint64_t)depth_key(d) << 32) | (less ? st.rank : ~st.rank);
-    return true;
+    return inside && d == d;
 }
 
 // Float -> 8 bits as Color4b::FromFloats: clamp, scale by 255, round half up.
@@ -1923,7 +1919,8 @@ __global__ void __launch_bounds__(128, S <= 4 ? 5 : 3) k_raster_ms(const __grid_
                     {
                         uint64_t k;
                         unsigned long long* slot = &key[s * 256 + y * 16 + x];
-                        if (sample_key(st, G, x, y, sample_offset(level, s), less, k) && k < *slot)
+                        const bool hit = sample_key(st, G, x, y, sample_offset(level, s), less, k);
+                        if (hit && k < *slot)
                             atomicMin(slot, (unsigned long long)k);
                     }
                 }
