@@ -1274,26 +1274,22 @@ __device__ __forceinline__ void stage_tri(const PassArgs& a, uint32_t entry, uin
 // accepted entries skip it) or the depth is NaN (never passes).
 __device__ __forceinline__ bool fragment_key(const StagedTri& s, int lx, int ly, bool less, uint64_t& key)
 {
+    // (no early exit: the lanes of a warp test different pixels, and the
+    // arithmetic of an uncovered one costs the warp nothing extra)
     const uint32_t fl = s.flags;
     const int l1 = wadd(wadd(wmul(s.A1, lx), wmul(s.D1, ly)), s.K1);
     const int l2 = wadd(wadd(wmul(s.A2, lx), wmul(s.D2, ly)), s.K2);
-    if (!(fl & (1u << 20)))
-    {
-        const int e0 = wadd(wadd(wmul(s.A0, lx), wmul(s.D0, ly)), s.K0);
-        const int e1 = wadd(l1, (fl & (1u << 21)) ? -1 : 0);
-        const int e2 = wadd(l2, (fl & (1u << 22)) ? -1 : 0);
-        if ((e0 | e1 | e2) < 0)
-            return false;
-    }
+    const int e0 = wadd(wadd(wmul(s.A0, lx), wmul(s.D0, ly)), s.K0);
+    const int e1 = wadd(l1, (fl & (1u << 21)) ? -1 : 0);
+    const int e2 = wadd(l2, (fl & (1u << 22)) ? -1 : 0);
+    const bool inside = (fl & (1u << 20)) || (e0 | e1 | e2) >= 0;
     // TriangleSSE::CalcBarycentricCoord / GetDepth (RasterTriangle.h:324-337)
     const float L0 = fmul(__int2float_rn(l1), s.invDet);
     const float L1 = fmul(__int2float_rn(l2), s.invDet);
     const float L2 = fsub(fsub(1.0f, L0), L1);
     const float d = fadd(fadd(fmul(L0, s.z0), fmul(L1, s.z1)), fmul(L2, s.z2));
-    if (d != d)
-        return false;
     key = ((uint64_t)depth_key(d) << 32) | (less ? s.rank : ~s.rank);
-    return true;
+    return inside && d == d;
 }
 
 constexpr int kRasterWarps = kRasterThreads / 32;
@@ -1575,7 +1571,9 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
                     const int x = rx0 + local - dy * rw, y = ry0 + dy;
                     uint64_t k;
                     // a plain read first: most fragments of deep overdraw lose
-                    if (fragment_key(s, x, y, less, k) && k < key[y * 16 + x])
+                    const bool hit = fragment_key(s, x, y, less, k);
+                    const unsigned long long cur = key[y * 16 + x];
+                    if (hit && k < cur)
                         atomicMin(&key[y * 16 + x], (unsigned long long)k);
                 }
             }
@@ -1597,7 +1595,9 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
                     const int dy = (int)(((uint32_t)p * inv) >> 16);
                     const int x = rx0 + p - dy * rw, y = ry0 + dy;
                     uint64_t k;
-                    if (fragment_key(s, x, y, less, k) && k < key[y * 16 + x])
+                    const bool hit = fragment_key(s, x, y, less, k);
+                    const unsigned long long cur = key[y * 16 + x];
+                    if (hit && k < cur)
                         key[y * 16 + x] = k;
                 }
                 __syncwarp();
@@ -1920,7 +1920,8 @@ __global__ void __launch_bounds__(128, S <= 4 ? 5 : 3) k_raster_ms(const __grid_
                         uint64_t k;
                         unsigned long long* slot = &key[s * 256 + y * 16 + x];
                         const bool hit = sample_key(st, G, x, y, sample_offset(level, s), less, k);
-                        if (hit && k < *slot)
+                        const unsigned long long cur = *slot;
+                        if (hit && k < cur)
                             atomicMin(slot, (unsigned long long)k);
                     }
                 }
