@@ -76,7 +76,7 @@ class Stats(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("small_region", ctypes.c_int), ("raster_variant", ctypes.c_int),
                 ("bin_blocks_per_sm", ctypes.c_int), ("raster_blocks_per_sm", ctypes.c_int),
-                ("bin_entries_per_triangle", ctypes.c_uint32)]
+                ("bin_entries_per_triangle", ctypes.c_uint32), ("item_entries", ctypes.c_int)]
 
 
 class View(ctypes.Structure):

@@ -22,6 +22,7 @@ GRID = {
     "small_region": [0, 4, 16, 64],
     "raster_variant": [0, 1, 2],
     "bin_blocks_per_sm": [4, 8, 16],
+    "item_entries": [128, 224],
 }
 
 

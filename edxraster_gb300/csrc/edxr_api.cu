@@ -489,7 +489,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     EDXR_CUDA(r->depth.ensure(4 * samples * std::max<uint64_t>(pixels, 1)));
     EDXR_CUDA(r->tri_id.ensure(4 * samples * std::max<uint64_t>(pixels, 1)));
     EDXR_CUDA(r->keybuf.ensure_zeroed(8 * samples * std::max<uint64_t>(pixels, 1), r->stream));
-    const uint64_t icap = item_capacity(tiles, r->bin_capacity);
+    const uint64_t icap = item_capacity(tiles, r->bin_capacity, (uint32_t)r->tuning.item_entries);
     EDXR_CUDA(r->items.ensure(sizeof(uint4) * icap));
     // a vertex stage when vertices are shared (on average by at least three
     // triangle corners) and their records stay in L2 for setup to gather
@@ -624,7 +624,7 @@ edxr_status sync_pass(edxr_renderer* r)
             a.bins = r->bins.as<uint32_t>();
             a.bin_tmp = r->bin_tmp.as<uint2>();
             a.bin_capacity = r->bin_capacity;
-            a.item_capacity = item_capacity(a.total_tiles, r->bin_capacity);
+            a.item_capacity = item_capacity(a.total_tiles, r->bin_capacity, (uint32_t)r->tuning.item_entries);
             EDXR_CUDA(r->items.ensure(sizeof(uint4) * a.item_capacity));
             a.items = r->items.as<uint4>();
         }
@@ -990,7 +990,8 @@ edxr_status edxr_set_tuning(edxr_renderer* r, const edxr_tuning* t)
         return fail(EDXR_ERR_INVALID_ARG, "NULL argument");
     if (t->small_region < 0 || t->small_region > 256 || t->raster_variant < 0 || t->raster_variant > 2 ||
         t->bin_blocks_per_sm < 1 || t->bin_blocks_per_sm > 64 || t->raster_blocks_per_sm < 0 ||
-        t->raster_blocks_per_sm > 32 || t->bin_entries_per_triangle < 1 || t->bin_entries_per_triangle > 1024)
+        t->raster_blocks_per_sm > 32 || t->bin_entries_per_triangle < 1 || t->bin_entries_per_triangle > 1024 ||
+        t->item_entries < 32 || t->item_entries > 1024)
         return fail(EDXR_ERR_INVALID_ARG, "tuning value out of range");
     DeviceGuard g(r->device);
     edxr_status s = sync_pass(r);
@@ -1000,6 +1001,7 @@ edxr_status edxr_set_tuning(edxr_renderer* r, const edxr_tuning* t)
     r->tuning.raster_variant = t->raster_variant;
     r->tuning.bin_blocks_per_sm = t->bin_blocks_per_sm;
     r->tuning.raster_blocks_per_sm = t->raster_blocks_per_sm;
+    r->tuning.item_entries = t->item_entries;
     r->bins_per_tri = t->bin_entries_per_triangle;
     return EDXR_OK;
 }
@@ -1028,6 +1030,7 @@ edxr_status edxr_get_tuning(edxr_renderer* r, edxr_tuning* t)
     t->bin_blocks_per_sm = r->tuning.bin_blocks_per_sm;
     t->raster_blocks_per_sm = r->tuning.raster_blocks_per_sm;
     t->bin_entries_per_triangle = r->bins_per_tri;
+    t->item_entries = r->tuning.item_entries;
     return EDXR_OK;
 }
 

@@ -26,7 +26,7 @@ constexpr uint32_t kNoTriangle = 0xFFFFFFFFu;
 // Raster work item: up to this many bin entries of one tile.  A tile with
 // more entries is split into several items whose winners are merged in a
 // per-pixel key buffer before the last of them shades the tile.
-constexpr uint32_t kItemEntries = 128;
+constexpr uint32_t kItemEntries = 128;  // default bin entries per raster work item (Tuning::item_entries)
 // Tile-count scan: tiles per block, and blocks (one status word each) of a pass.
 constexpr int kScanItems = 4;
 constexpr int kScanThreads = 256;
@@ -47,8 +47,11 @@ constexpr int kStripeStride = 32;
 constexpr int kStripeBase = 16;
 constexpr int kCounters = kStripeBase + kBinStripes * kStripeStride;  // words of PassArgs::counters
 __host__ __device__ constexpr uint64_t stripe_slots(uint64_t bin_capacity) { return bin_capacity / kBinStripes; }
-// Work items of a pass: one per tile plus one per kItemEntries bin entries.
-constexpr uint64_t item_capacity(uint64_t tiles, uint64_t bin_capacity) { return tiles + bin_capacity / kItemEntries + 1; }
+// Work items of a pass: one per tile plus one per item_entries bin entries.
+constexpr uint64_t item_capacity(uint64_t tiles, uint64_t bin_capacity, uint32_t item_entries = kItemEntries)
+{
+    return tiles + bin_capacity / item_entries + 1;
+}
 // 3 + one vertex per clip plane is 9 in exact arithmetic; rounding on nearly
 // collinear vertices can add a few more, so the working polygon has room.
 constexpr int kMaxPolygon = 16;
@@ -143,6 +146,7 @@ struct Tuning
     int raster_variant;   // 0/1: k_raster with the triangle-parallel path (3 / 5 blocks per SM), 2: pixel-parallel only
     int bin_blocks_per_sm;
     int raster_blocks_per_sm;  // 0 = as many as fit
+    int item_entries;     // bin entries per raster work item; items of at least 3/4 of it are handed out first
     // Failure test of the scan's bounded wait (edxr_debug_scan_stall): scan
     // block scan_stall_block (-1: none) does not publish its sum, and a wait
     // gives up after scan_spin_limit polls (0: kScanSpinLimit).
@@ -181,7 +185,7 @@ struct PassArgs
                              // unsorted bin list (kCounters words)
     unsigned long long* scan_status;  // per scan block (scan_blocks(total_tiles) words)
     uint4* items;            // raster work items (tile | split flag, first entry, end entry, 0), one per
-                             // kItemEntries-entry slice: heavy ones from the front, light ones from the back
+                             // item_entries-entry slice: heavy ones from the front, light ones from the back
     uint64_t item_capacity;
     unsigned long long* keybuf;  // per pixel: ~(smallest key) of split tiles, 0 between passes
     DeviceStatus* status;

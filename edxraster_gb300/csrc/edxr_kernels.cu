@@ -24,7 +24,6 @@ constexpr int kRasterThreads = 256;    // 8 warps, each on its own work items
 constexpr uint32_t kBigChunk = 128;    // unsorted-list slots a k_bin_big warp reserves at a time
 constexpr uint32_t kEmptySlot = 0xFFFFFFFFu;
 constexpr uint32_t kSplitTile = 0x80000000u;  // item tag: the tile has several items (tiles < 2^24)
-constexpr uint32_t kHeavyItem = 96;    // raster items with this many entries are handed out first
 
 // Clip-space position of vertex v: clip = MVP * (p, 1) (DefaultVertexShader,
 // Shader.h:40-49).
@@ -927,8 +926,8 @@ __global__ void __launch_bounds__(256, 4) k_bin_big(PassArgs a)
 // the range, kScanPrefix | sum of everything up to the range's end).
 //
 // The same pass lists the raster work items: one per tile (an empty tile's
-// item writes its background) plus one per further kItemEntries entries.
-// Items of at least kHeavyItem entries are listed from the front of the
+// item writes its background) plus one per further tune.item_entries entries.
+// Items of at least 3/4 of that are listed from the front of the
 // item array, the lighter ones from its back, and the queue hands out the
 // front list first: the heavy work starts early instead of forming the tail.
 __device__ __forceinline__ uint32_t padded(uint32_t c) { return (c + 3u) & ~3u; }
@@ -1038,6 +1037,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
     const bool dropped =
         __syncthreads_or(threadIdx.x < (uint32_t)kBinStripes &&
                          *(volatile uint32_t*)stripe_counter(a, threadIdx.x) > stripe_slots(a.bin_capacity)) != 0;
+    // entries per work item; items of at least 3/4 of that are heavy
+    const uint32_t E = (uint32_t)a.tune.item_entries, heavy_min = E - E / 4;
     uint32_t run = prefix + incl - sum;
     uint32_t nheavy = 0, nlight = 0;
     uint32_t start[kScanItems], n[kScanItems];
@@ -1056,9 +1057,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
                 c = 0;
                 a.tile_count[i] = 0;
             }
-            n[k] = max(1u, (c + kItemEntries - 1) / kItemEntries);
+            n[k] = max(1u, (c + E - 1) / E);
             // only the last item of a tile can be light
-            const uint32_t light = (c - (n[k] - 1) * kItemEntries) < kHeavyItem ? 1u : 0u;
+            const uint32_t light = (c - (n[k] - 1) * E) < heavy_min ? 1u : 0u;
             nlight += light;
             nheavy += n[k] - light;
             cnt[k] = c;
@@ -1093,18 +1094,17 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
         const uint32_t i = base + k;
         if (i >= a.total_tiles)
             continue;
-        const bool light = (cnt[k] - (n[k] - 1) * kItemEntries) < kHeavyItem;
+        const bool light = (cnt[k] - (n[k] - 1) * E) < heavy_min;
         const uint32_t heavy = n[k] - (light ? 1u : 0u);
         const uint32_t end = start[k] + cnt[k];
         const uint32_t tag = i | (n[k] > 1 ? kSplitTile : 0u);
         for (uint32_t j = 0; j < heavy; j++, hbase++)
             if (hbase < a.item_capacity)
-                a.items[hbase] = make_uint4(tag, start[k] + j * kItemEntries,
-                                            min(end, start[k] + (j + 1) * kItemEntries), 0u);
+                a.items[hbase] = make_uint4(tag, start[k] + j * E, min(end, start[k] + (j + 1) * E), 0u);
         if (light)
         {
             if (lbase < a.item_capacity)
-                a.items[a.item_capacity - 1 - lbase] = make_uint4(tag, start[k] + (n[k] - 1) * kItemEntries, end, 0u);
+                a.items[a.item_capacity - 1 - lbase] = make_uint4(tag, start[k] + (n[k] - 1) * E, end, 0u);
             lbase++;
         }
     }
@@ -1143,7 +1143,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
 
 // -------------------------------------------------------------------------
 // Raster: persistent warps take work items from a queue.  An item is one
-// 16x16 tile's slice of at most kItemEntries bin entries; the warp keeps one
+// 16x16 tile's slice of at most tune.item_entries bin entries; the warp keeps one
 // 64-bit key per pixel of the tile in shared memory.  The winner of the
 // reference's sequential depth test at a pixel is the fragment with the
 // smallest key (depth key << 32 | submission rank term): for LEQUAL the last
@@ -2088,6 +2088,7 @@ Tuning default_tuning()
     t.raster_variant = 1;
     t.bin_blocks_per_sm = 8;
     t.raster_blocks_per_sm = 0;
+    t.item_entries = (int)kItemEntries;
     t.scan_stall_block = -1;
     t.scan_spin_limit = 0;
     return t;

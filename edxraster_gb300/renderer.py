@@ -311,7 +311,7 @@ class Renderer:
         return s
 
     TUNING_FIELDS = ("small_region", "raster_variant", "bin_blocks_per_sm", "raster_blocks_per_sm",
-                     "bin_entries_per_triangle")
+                     "bin_entries_per_triangle", "item_entries")
 
     def SetTuning(self, tuning: dict):
         cur = self.GetTuning()

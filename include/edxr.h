@@ -297,6 +297,9 @@ typedef struct edxr_tuning
     int bin_blocks_per_sm;        /* grid of the per-triangle binning kernels */
     int raster_blocks_per_sm;     /* persistent raster blocks per SM; 0 = the occupancy maximum */
     uint32_t bin_entries_per_triangle;  /* initial bin-buffer capacity per triangle (grows on overflow) */
+    int item_entries;             /* bin entries per raster work item (32..1024, default 128): a tile with
+                                     more is split over several items that merge their keys; items of at
+                                     least 3/4 of it are handed out first */
 } edxr_tuning;
 
 edxr_status edxr_set_tuning(edxr_renderer* r, const edxr_tuning* tuning);
