@@ -52,8 +52,13 @@ def time_calls(r, stream, render, steps, warmup, flush=None):
     return total / steps
 
 
-def tune(r, stream, render, triangles: int, steps: int = 5, warmup: int = 2, flush=None, grid=None):
-    """Return (best tuning dict, [(candidate, ms), ...])."""
+def tune(r, stream, render, triangles: int, steps: int = 5, warmup: int = 2, flush=None, grid=None, finalists=6,
+         rounds=3):
+    """Return (best tuning dict, [(candidate, ms), ...]).  Every candidate of
+    the grid is timed once; the `finalists` fastest are timed again `rounds`
+    times, interleaved, and the one with the lowest median wins (a single
+    timing of a sub-millisecond frame is too noisy to rank close candidates)."""
+    import statistics
     grid = grid or GRID
     keys = list(grid)
     table = []
@@ -61,7 +66,15 @@ def tune(r, stream, render, triangles: int, steps: int = 5, warmup: int = 2, flu
         cand = dict(zip(keys, values))
         r.SetTuning(cand)
         table.append((cand, time_calls(r, stream, render, steps, warmup, flush)))
-    best = dict(min(table, key=lambda x: x[1])[0])
+    final = [c for c, _ in sorted(table, key=lambda x: x[1])[:finalists]]
+    times = [[] for _ in final]
+    for _ in range(rounds):
+        for i, cand in enumerate(final):
+            r.SetTuning(cand)
+            times[i].append(time_calls(r, stream, render, 2 * steps, warmup, flush))
+    medians = [statistics.median(t) for t in times]
+    best = dict(final[min(range(len(final)), key=lambda i: medians[i])])
+    table = [(c, medians[final.index(c)] if c in final else ms) for c, ms in table]
     r.SetTuning(best)
     render()
     r.Synchronize()
