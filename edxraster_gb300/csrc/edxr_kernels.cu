@@ -1498,6 +1498,23 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
         // (a frame whose entries overflowed has empty items: rendered again by the host)
         const uint32_t e0 = item.y, e1 = item.z;
         const bool split = (item.x & kSplitTile) != 0;
+        if (e0 == e1 && !split)
+        {
+            // a tile with no bin entry: its background, with no key
+            for (int k = 0; k < 8; k++)
+            {
+                const int p = (int)lane + 32 * k;
+                const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
+                if (px < f.width && py < f.height)
+                {
+                    const uint64_t pix = f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px;
+                    a.color[pix] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    a.depth[pix] = 1.0f;
+                    a.tri_id[pix] = kNoTriangle;
+                }
+            }
+            continue;
+        }
 
         // clear depth 1.0 with no triangle: rank term ~0 (LEQUAL) or 0 (LESS)
         const unsigned long long clear = ((unsigned long long)0xBF800000u << 32) | (less ? 0u : 0xFFFFFFFFu);
@@ -1851,6 +1868,26 @@ __global__ void __launch_bounds__(128, S <= 4 ? 5 : 3) k_raster_ms(const __grid_
         // (a frame whose entries overflowed has empty items: rendered again by the host)
         const uint32_t e0 = item.y, e1 = item.z;
         const bool split = (item.x & kSplitTile) != 0;
+        if (e0 == e1 && !split)
+        {
+            // a tile with no bin entry: its background, with no key
+            for (int k = 0; k < 8; k++)
+            {
+                const int p = (int)lane + 32 * k;
+                const int px = (tileX << 4) + (p & 15), py = (tileY << 4) + (p >> 4);
+                if (px < f.width && py < f.height)
+                {
+                    const uint64_t pix = f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px;
+                    a.color[pix] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    for (int s = 0; s < S; s++)
+                    {
+                        a.depth[s * plane + pix] = 1.0f;
+                        a.tri_id[s * plane + pix] = kNoTriangle;
+                    }
+                }
+            }
+            continue;
+        }
         const unsigned long long clear = ((unsigned long long)0xBF800000u << 32) | (less ? 0u : 0xFFFFFFFFu);
         for (int k = (int)lane; k < 256 * S; k += 32)
             key[k] = clear;
