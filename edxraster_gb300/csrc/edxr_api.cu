@@ -431,9 +431,11 @@ void fill_frame(FrameDesc& f, const edxr_mesh& m, const Camera& cam, const Shadi
 edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t height, int msaa_log2 = 0)
 {
     uint64_t tv = 0, tt = 0, tiles = 0;
+    bool equal_tiles = true;
     for (uint32_t i = 0; i < n; i++)
     {
         FrameDesc& f = r->frames_host[i];
+        equal_tiles = equal_tiles && (uint64_t)f.tdx * f.tdy == (uint64_t)r->frames_host[0].tdx * r->frames_host[0].tdy;
         f.vtx_base = (uint32_t)tv;
         f.tri_base = (uint32_t)tt;
         f.tile_base = (uint32_t)tiles;
@@ -506,6 +508,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.tune = r->tuning;
     a.frames = r->frames.as<FrameDesc>();
     a.num_frames = n;
+    a.tiles_per_frame = equal_tiles && n > 1 ? (uint32_t)(tiles / n) : 0u;  // (one frame: no search)
     a.total_vertices = (uint32_t)tv;
     a.vrecs = vertex_stage ? r->vrecs.as<int4>() : nullptr;
     a.total_tris = (uint32_t)tt;

@@ -1490,7 +1490,9 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
     {
         const uint4 item = a.items[q < nheavy ? q : (uint32_t)(a.item_capacity - 1 - (q - nheavy))];
         const uint32_t tile = item.x & ~kSplitTile;
-        const uint32_t fi = find_frame(a.frames, a.num_frames, tile, [](const FrameDesc& f) { return f.tile_base; });
+        const uint32_t fi = a.tiles_per_frame ? tile / a.tiles_per_frame
+                                              : find_frame(a.frames, a.num_frames, tile,
+                                                           [](const FrameDesc& f) { return f.tile_base; });
         const FrameDesc& f = a.frames[fi];
         const uint32_t lt = tile - f.tile_base;
         const int tileX = (int)(lt % (uint32_t)f.tdx), tileY = (int)(lt / (uint32_t)f.tdx);
@@ -1860,7 +1862,9 @@ __global__ void __launch_bounds__(128, S <= 4 ? 5 : 3) k_raster_ms(const __grid_
     {
         const uint4 item = a.items[q < nheavy ? q : (uint32_t)(a.item_capacity - 1 - (q - nheavy))];
         const uint32_t tile = item.x & ~kSplitTile;
-        const uint32_t fi = find_frame(a.frames, a.num_frames, tile, [](const FrameDesc& f) { return f.tile_base; });
+        const uint32_t fi = a.tiles_per_frame ? tile / a.tiles_per_frame
+                                              : find_frame(a.frames, a.num_frames, tile,
+                                                           [](const FrameDesc& f) { return f.tile_base; });
         const FrameDesc& f = a.frames[fi];
         const uint32_t lt = tile - f.tile_base;
         const int tileX = (int)(lt % (uint32_t)f.tdx), tileY = (int)(lt / (uint32_t)f.tdx);

@@ -176,6 +176,7 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
     a.tune = default_tuning();
     a.frames = reinterpret_cast<const FrameDesc*>(base + kOffFrame);
     a.num_frames = 1;
+    a.tiles_per_frame = 0;  // (one frame: the search is one step)
     a.total_vertices = f.nv;
     a.total_tris = f.nt;
     a.total_tiles = tiles;
