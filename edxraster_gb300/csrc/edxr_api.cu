@@ -220,7 +220,8 @@ struct edxr_renderer
     Shading shading;
     Camera cam;
 
-    DevBuf frames, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, tile_zocc, bins, bin_tmp, big_list, counters,
+    DevBuf frames, frame_of_block, rtris, polys, clip_list, tile_count, tile_offset, tile_cursor, tile_zocc, bins, bin_tmp,
+        big_list, counters,
         status;
     DevBuf color, depth, tri_id, back8, diff_scratch, tri_first, items, keybuf, vrecs;
     // texture slots (edxr_set_textures): descriptors and the texel pool with mip chains
@@ -509,6 +510,11 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.frames = r->frames.as<FrameDesc>();
     a.num_frames = n;
     a.tiles_per_frame = equal_tiles && n > 1 ? (uint32_t)(tiles / n) : 0u;  // (one frame: no search)
+    if (n > 1)
+    {
+        EDXR_CUDA(r->frame_of_block.ensure(4 * (tt / 256 + 1)));
+        a.frame_of_block = r->frame_of_block.as<uint32_t>();
+    }
     a.total_vertices = (uint32_t)tv;
     a.vrecs = vertex_stage ? r->vrecs.as<int4>() : nullptr;
     a.total_tris = (uint32_t)tt;
@@ -709,7 +715,7 @@ edxr_status edxr_destroy(edxr_renderer* r)
         cudaEventSynchronize(r->done);
     if (r->graph)
         cudaGraphExecDestroy(r->graph);
-    DevBuf* bufs[] = { &r->frames, &r->rtris, &r->polys, &r->clip_list, &r->tile_count, &r->tile_offset,
+    DevBuf* bufs[] = { &r->frames, &r->frame_of_block, &r->rtris, &r->polys, &r->clip_list, &r->tile_count, &r->tile_offset,
                        &r->tile_cursor, &r->tile_zocc, &r->bins, &r->bin_tmp, &r->big_list, &r->counters, &r->status, &r->color,
                        &r->depth, &r->tri_id, &r->back8, &r->diff_scratch, &r->tri_first, &r->items,
                        &r->keybuf, &r->tex_desc, &r->tex_texels, &r->vrecs };

@@ -161,6 +161,7 @@ struct PassArgs
     const FrameDesc* frames;
     uint32_t num_frames;
     uint32_t tiles_per_frame;  // every frame's tile count when they are equal (then frame = tile / it), else 0
+    uint32_t* frame_of_block;  // several frames: the frame of triangle 256 b, per b (filled by k_clear); else NULL
     uint32_t total_vertices;
     int4* vrecs;             // per flattened vertex: setup record (vertex stage), or NULL: setup projects in place
     uint32_t total_tris;

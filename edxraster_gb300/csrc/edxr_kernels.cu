@@ -63,6 +63,12 @@ __global__ void k_clear(PassArgs a)
             const FrameDesc& f = a.frames[fi];
             a.vrecs[i] = vertex_record(f, i - f.vtx_base);
         }
+    // several frames: the frame of every 256th triangle, where setup's
+    // frame lookup starts (instead of a search over every frame)
+    if (a.frame_of_block)
+        for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b <= (a.total_tris >> 8); b += stride)
+            a.frame_of_block[b] =
+                find_frame(a.frames, a.num_frames, b << 8, [](const FrameDesc& f) { return f.tri_base; });
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= a.total_tiles; i += stride)
     {
         a.tile_count[i] = 0;
@@ -209,6 +215,19 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, int n)
     return __shfl_sync(0xffffffffu, base, 31) + (uint32_t)(incl - n);
 }
 
+// Frame of flattened input triangle gi: from its 256-block's frame, forward
+// over the frames that start at or before it (find_frame's answer: the last
+// frame whose first triangle is at or before gi).
+__device__ __forceinline__ uint32_t frame_of_triangle(const PassArgs& a, uint32_t gi)
+{
+    if (!a.frame_of_block)
+        return find_frame(a.frames, a.num_frames, gi, [](const FrameDesc& f) { return f.tri_base; });
+    uint32_t fi = a.frame_of_block[gi >> 8];
+    while (fi + 1 < a.num_frames && a.frames[fi + 1].tri_base <= gi)
+        fi++;
+    return fi;
+}
+
 // Setup of the triangles that need no clipping (all clip codes zero), one
 // thread per input triangle; triangles that straddle a clip plane are queued
 // for k_clip, triangles outside one plane are dropped (Clipper.h:103-109).
@@ -227,7 +246,7 @@ __global__ void __launch_bounds__(256, 6) k_setup(PassArgs a)
     RTri t;
     if (gi < a.total_tris)
     {
-        fi = find_frame(a.frames, a.num_frames, gi, [](const FrameDesc& f) { return f.tri_base; });
+        fi = frame_of_triangle(a, gi);
         const FrameDesc& f = a.frames[fi];
         tri = gi - f.tri_base;
         const uint32_t i0 = __ldg(f.indices + 3 * (size_t)tri);
@@ -503,7 +522,7 @@ __device__ __forceinline__ void clip_groups(const PassArgs& a, uint32_t nq)
     if (q < nq)
     {
         gi = a.clip_list[q];
-        fi = find_frame(a.frames, a.num_frames, gi, [](const FrameDesc& f) { return f.tri_base; });
+        fi = frame_of_triangle(a, gi);
         const FrameDesc& f = a.frames[fi];
         tri = gi - f.tri_base;
         n = 3;
@@ -617,7 +636,7 @@ __device__ __forceinline__ void clip_lanes(const PassArgs& a, uint32_t nq, float
         if (lane < per && q64 < nq)
         {
             gi = a.clip_list[q];
-            fi = find_frame(a.frames, a.num_frames, gi, [](const FrameDesc& f) { return f.tri_base; });
+            fi = frame_of_triangle(a, gi);
             const FrameDesc& f = a.frames[fi];
             tri = gi - f.tri_base;
             const float4 c0 = clip_position(f, __ldg(f.indices + 3 * (size_t)tri));
