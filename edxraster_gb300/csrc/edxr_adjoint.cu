@@ -28,8 +28,18 @@ namespace {
 
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ uint32_t frame_of_pixel(const FrameDesc* frames, uint32_t n, uint64_t p)
+// Frame of flattened output pixel p: one division when the pass's frames
+// share one resolution (tiles_per_frame set: the batched pass), else a
+// search over the frames' first pixels.
+__device__ __forceinline__ uint32_t frame_of_pixel(const PassArgs& a, uint64_t p)
 {
+    if (a.tiles_per_frame)
+    {
+        const uint64_t per_frame = a.total_pixels / a.num_frames;
+        return a.total_pixels <= 0xFFFFFFFFull ? (uint32_t)p / (uint32_t)per_frame : (uint32_t)(p / per_frame);
+    }
+    const FrameDesc* frames = a.frames;
+    const uint32_t n = a.num_frames;
     uint32_t lo = 0, hi = n - 1;
     while (lo < hi)
     {
@@ -246,7 +256,7 @@ __global__ void __launch_bounds__(kThreads) k_shade_visible(PassArgs a, uint64_t
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= total)
         return;
-    const FrameDesc& f = a.frames[frame_of_pixel(a.frames, a.num_frames, i)];
+    const FrameDesc& f = a.frames[frame_of_pixel(a, i)];
     const uint64_t local = i - f.pix_base;
     const int px = (int)(local % (uint32_t)f.width), py = (int)(local / (uint32_t)f.width);
     const uint32_t tri = a.tri_id[i];
@@ -279,7 +289,7 @@ __global__ void __launch_bounds__(kThreads) k_backward(PassArgs a, uint64_t tota
     float dks = 0.0f, dshin = 0.0f;
     if (i < total)
     {
-        const FrameDesc& f = a.frames[frame_of_pixel(a.frames, a.num_frames, i)];
+        const FrameDesc& f = a.frames[frame_of_pixel(a, i)];
         const uint64_t local = i - f.pix_base;
         const int px = (int)(local % (uint32_t)f.width), py = (int)(local / (uint32_t)f.width);
         const uint32_t tri = a.tri_id[i];
