@@ -474,7 +474,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     const uint64_t nscan = scan_blocks(tiles);
     EDXR_CUDA(r->frames.ensure(sizeof(FrameDesc) * n));
     EDXR_CUDA(r->tri_first.ensure(4 * std::max<uint64_t>(tt, 1)));
-    EDXR_CUDA(r->rtris.ensure(sizeof(RTri) * rcap));
+    EDXR_CUDA(r->rtris.ensure((sizeof(RTri) + 4) * rcap));  // the records, then their depth bounds
     EDXR_CUDA(r->polys.ensure(sizeof(ClipPoly) * pcap));
     EDXR_CUDA(r->clip_list.ensure(4 * pcap));
     EDXR_CUDA(r->tile_count.ensure(4 * (tiles + 1)));
@@ -520,6 +520,7 @@ edxr_status launch_frames(edxr_renderer* r, uint32_t n, uint32_t width, uint32_t
     a.total_tris = (uint32_t)tt;
     a.total_tiles = (uint32_t)tiles;
     a.rtris = r->rtris.as<RTri>();
+    a.rtri_zlo = reinterpret_cast<uint32_t*>(a.rtris + rcap);
     a.rtri_capacity = (uint32_t)std::min<uint64_t>(rcap, 0xFFFFFFFFu);
     a.polys = r->polys.as<ClipPoly>();
     a.clip_list = r->clip_list.as<uint32_t>();
@@ -603,8 +604,9 @@ edxr_status sync_pass(edxr_renderer* r)
         if (st.overflow & 2u)
         {
             r->rtri_cap = std::min<uint64_t>((uint64_t)st.rtri_slots + st.rtri_slots / 4 + 1024, 0xFFFFFFF0u);
-            EDXR_CUDA(r->rtris.ensure(sizeof(RTri) * r->rtri_cap));
+            EDXR_CUDA(r->rtris.ensure((sizeof(RTri) + 4) * r->rtri_cap));
             a.rtris = r->rtris.as<RTri>();
+            a.rtri_zlo = reinterpret_cast<uint32_t*>(a.rtris + r->rtri_cap);
             a.rtri_capacity = (uint32_t)r->rtri_cap;
         }
         if (st.overflow & 4u)

@@ -167,15 +167,17 @@ struct PassArgs
     uint32_t total_tris;
     uint32_t total_tiles;
     RTri* rtris;             // slot i < total_tris: unclipped input triangle i; then fan pieces (counters[0])
+    uint32_t* rtri_zlo;      // per raster-triangle slot: the lower bound of its depth keys (zmin_key)
     uint32_t rtri_capacity;
     ClipPoly* polys;
     uint32_t poly_capacity;  // also the capacity of clip_list
     uint32_t* clip_list;     // input triangles (flattened) that straddle a clip plane
-    uint32_t* tile_count;    // total_tiles + 1
+    uint32_t* tile_count;    // total_tiles + 1; counts until the scan, then (zeroed by it) the entries of a split
+                             // tile its items have rastered
     uint32_t* tile_offset;   // total_tiles + 1 (exclusive scan of padded counts)
     uint32_t* tile_zocc;     // total_tiles + 1; per tile the least far-depth key of the triangles accepted
                              // over it whole (entries beyond it are hidden), ~0 for none
-    uint32_t* tile_cursor;   // total_tiles + 1; the scatter's cursors, then entries of split tiles not yet rastered
+    uint32_t* tile_cursor;   // total_tiles + 1; the scatter's cursors: after it, the entries each bin holds
     uint32_t* bins;
     uint2* bin_tmp;          // decided (tile, entry) pairs before the scatter, bin_capacity of them
     uint64_t bin_capacity;

@@ -161,6 +161,21 @@ __device__ __forceinline__ void bin_small(const PassArgs& a, const FrameDesc& f,
         }
 }
 
+// Lower bound (as a depth key) of every depth the reference computes for the
+// triangle at a pixel it rasterizes, or 0 (never culled) when the triangle is
+// large enough for int32 edge values to wrap.  Without wraparound the
+// barycentrics of rasterized pixels are within a few ulps of [0, 1], so the
+// computed depth is at least min(z) minus a few ulps of the |z| sum.
+__device__ __forceinline__ uint32_t zmin_key(const RTri& t, bool wf)
+{
+    if (!wf)
+        return 0u;
+    const float zmin = fminf(t.z0, fminf(t.z1, t.z2));
+    const float margin = 2e-6f * (fabsf(t.z0) + fabsf(t.z1) + fabsf(t.z2)) + 1e-30f;
+    const float lo = zmin - margin;
+    return (lo == lo) ? depth_key(lo) : 0u;
+}
+
 // Stripe of the unsorted bin list a warp appends to, its fill counter and
 // its first slot.
 __device__ __forceinline__ uint32_t warp_stripe()
@@ -338,6 +353,7 @@ __global__ void __launch_bounds__(256, 6) k_setup(PassArgs a)
         t.meta |= fi << 12;
         t.poly = kUnclipped;
         a.rtris[gi] = t;
+        a.rtri_zlo[gi] = zmin_key(t, wrap_free(t));
     }
     bin_big_append(a, gi, nOut && big);
     if (nOut && nent)
@@ -474,6 +490,7 @@ __device__ __forceinline__ void clip_piece(const PassArgs& a, bool has, uint32_t
         tk.poly = (poly << 4) | (fan + 1u);
         kept = true;
         a.rtris[ri] = tk;
+        a.rtri_zlo[ri] = zmin_key(tk, wrap_free(tk));
         const BinGeom bg = bin_geom(tk, f);
         big = !bg.small;
         if (bg.small)
@@ -720,7 +737,8 @@ __global__ void __launch_bounds__(kClipThreads) k_clip(PassArgs a)
 }
 
 // Scatter of the unsorted entries into their bins (after the scan); empty
-// slots are skipped.
+// slots and entries hidden behind their tile's occluder are skipped, so a
+// bin holds its tile's first tile_cursor entries.
 __global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
 {
     // the filled parts of the stripes (slots past a stripe's end were
@@ -763,6 +781,16 @@ __global__ void __launch_bounds__(256) k_bin_move(PassArgs a)
             for (uint32_t st = 16; st >= 1; st >>= 1)
                 if (s_first[r + st] <= j) r += st;
             e = a.bin_tmp[(uint64_t)r * R + (j - s_first[r])];
+            // an entry wholly behind its tile's occluder is dropped: the
+            // raster's depth bound would skip it at staging (its nearest
+            // depth beyond min(occluder bound, clear depth))
+            if (e.x != kEmptySlot)
+            {
+                const uint32_t zocc = a.tile_zocc[e.x];
+                const uint32_t ri = e.y >> 2;
+                if (zocc != 0xFFFFFFFFu && ri < a.rtri_capacity && a.rtri_zlo[ri] > min(zocc, 0xBF800000u))
+                    e.x = kEmptySlot;
+            }
         }
         uint32_t base = 0;
         if (a.vrecs)
@@ -1071,11 +1099,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(PassArgs a)
         {
             a.tile_offset[i] = run;
             uint32_t c = cnt[k];
+            a.tile_count[i] = 0;  // from here on: the split tile's rastered entries
             if (dropped || (uint64_t)run + c > a.bin_capacity)
-            {
                 c = 0;
-                a.tile_count[i] = 0;
-            }
             n[k] = max(1u, (c + E - 1) / E);
             // only the last item of a tile can be light
             const uint32_t light = (c - (n[k] - 1) * E) < heavy_min ? 1u : 0u;
@@ -1191,21 +1217,6 @@ struct __align__(16) StagedTri
 };
 
 constexpr uint32_t kEmptyRegion = 16u | (16u << 10);  // lx0 = ly0 = 16 > lx1 = ly1 = 0
-
-// Lower bound (as a depth key) of every depth the reference computes for the
-// triangle at a pixel it rasterizes, or 0 (never culled) when the triangle is
-// large enough for int32 edge values to wrap.  Without wraparound the
-// barycentrics of rasterized pixels are within a few ulps of [0, 1], so the
-// computed depth is at least min(z) minus a few ulps of the |z| sum.
-__device__ __forceinline__ uint32_t zmin_key(const RTri& t, bool wf)
-{
-    if (!wf)
-        return 0u;
-    const float zmin = fminf(t.z0, fminf(t.z1, t.z2));
-    const float margin = 2e-6f * (fabsf(t.z0) + fabsf(t.z1) + fabsf(t.z2)) + 1e-30f;
-    const float lo = zmin - margin;
-    return (lo == lo) ? depth_key(lo) : 0u;
-}
 
 // Tile-relative edge equations, barycentric numerators and region of one
 // bin entry.
@@ -1348,12 +1359,12 @@ __device__ __forceinline__ uint32_t raster_triangle_of(const PassArgs& a, uint32
     return ri < nr ? ri : kNoTriangle;
 }
 
-// *p -= v at device scope with acquire-release semantics; returns the old
-// value.  A split tile's items count its entries down with it (see k_raster).
-__device__ __forceinline__ uint32_t atomic_sub_acq_rel(uint32_t* p, uint32_t v)
+// *p += v at device scope with acquire-release semantics; returns the old
+// value.  A split tile's items count its rastered entries with it (see k_raster).
+__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v)
 {
     uint32_t old;
-    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;\n" : "=r"(old) : "l"(p), "r"(0u - v) : "memory");
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;\n" : "=r"(old) : "l"(p), "r"(v) : "memory");
     return old;
 }
 
@@ -1517,8 +1528,17 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
         const int tileX = (int)(lt % (uint32_t)f.tdx), tileY = (int)(lt / (uint32_t)f.tdx);
         const bool less = f.depth_func == 1;
         // (a frame whose entries overflowed has empty items: rendered again by the host)
-        const uint32_t e0 = item.y, e1 = item.z;
-        const bool split = (item.x & kSplitTile) != 0;
+        bool split = (item.x & kSplitTile) != 0;
+        // the item's range within the entries its bin kept (the scatter drops
+        // entries hidden behind the tile's occluder)
+        const uint32_t kept = a.tile_cursor[tile], bin0 = a.tile_offset[tile];
+        const uint32_t e1 = min(item.z, bin0 + kept), e0 = min(item.y, e1);
+        if (split && e0 == e1)
+        {
+            if (item.y != bin0 || kept != 0)
+                continue;  // the tile's kept entries are in its other items
+            split = false;  // it kept none: its first item writes the background
+        }
         if (e0 == e1 && !split)
         {
             // a tile with no bin entry: its background, with no key
@@ -1651,8 +1671,9 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
         }
 
         // A tile split into several items merges its keys in the key buffer;
-        // the item that finishes last (the tile's cursor, equal to its entry
-        // count after the scatter, counted down to zero) shades the tile.
+        // the item that finishes last (the one whose entries bring the tile's
+        // rastered count, zeroed by the scan, to the entries its bin kept)
+        // shades the tile.
         bool shade = true;
         if (split)
         {
@@ -1665,15 +1686,15 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
                 if (px < f.width && py < f.height && kk < clear)
                     atomicMax(&a.keybuf[f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px], ~kk);
             }
-            // The countdown is one acquire-release atomic: the lanes' merges
+            // The count is one acquire-release atomic: the lanes' merges
             // happen before it (warp barrier, then lane 0's release), and
-            // the item that counts the tile down to zero acquires every
-            // other item's merges before it reads them back.
+            // the item that completes the tile acquires every other item's
+            // merges before it reads them back.
             __syncwarp();
-            uint32_t left = 0;
+            uint32_t done = 0;
             if (lane == 0)
-                left = atomic_sub_acq_rel(&a.tile_cursor[tile], e1 - e0) - (e1 - e0);
-            shade = __shfl_sync(0xffffffffu, left, 0) == 0;
+                done = atomic_add_acq_rel(&a.tile_count[tile], e1 - e0) + (e1 - e0);
+            shade = __shfl_sync(0xffffffffu, done, 0) == kept;
             __syncwarp();  // lane 0's acquire, then every lane's reads
             if (shade)
             {
@@ -1889,8 +1910,17 @@ __global__ void __launch_bounds__(128, S <= 4 ? 5 : 3) k_raster_ms(const __grid_
         const int tileX = (int)(lt % (uint32_t)f.tdx), tileY = (int)(lt / (uint32_t)f.tdx);
         const bool less = f.depth_func == 1;
         // (a frame whose entries overflowed has empty items: rendered again by the host)
-        const uint32_t e0 = item.y, e1 = item.z;
-        const bool split = (item.x & kSplitTile) != 0;
+        bool split = (item.x & kSplitTile) != 0;
+        // the item's range within the entries its bin kept (the scatter drops
+        // entries hidden behind the tile's occluder)
+        const uint32_t kept = a.tile_cursor[tile], bin0 = a.tile_offset[tile];
+        const uint32_t e1 = min(item.z, bin0 + kept), e0 = min(item.y, e1);
+        if (split && e0 == e1)
+        {
+            if (item.y != bin0 || kept != 0)
+                continue;  // the tile's kept entries are in its other items
+            split = false;  // it kept none: its first item writes the background
+        }
         if (e0 == e1 && !split)
         {
             // a tile with no bin entry: its background, with no key
@@ -2007,12 +2037,12 @@ __global__ void __launch_bounds__(128, S <= 4 ? 5 : 3) k_raster_ms(const __grid_
                 if (px < f.width && py < f.height && kk < clear)
                     atomicMax(&a.keybuf[s * plane + f.pix_base + (uint64_t)py * (uint32_t)f.width + (uint32_t)px], ~kk);
             }
-            // acquire-release countdown, as in k_raster
+            // acquire-release count, as in k_raster
             __syncwarp();
-            uint32_t left = 0;
+            uint32_t done = 0;
             if (lane == 0)
-                left = atomic_sub_acq_rel(&a.tile_cursor[tile], e1 - e0) - (e1 - e0);
-            shade = __shfl_sync(0xffffffffu, left, 0) == 0;
+                done = atomic_add_acq_rel(&a.tile_count[tile], e1 - e0) + (e1 - e0);
+            shade = __shfl_sync(0xffffffffu, done, 0) == kept;
             __syncwarp();  // lane 0's acquire, then every lane's reads
             if (shade)
             {

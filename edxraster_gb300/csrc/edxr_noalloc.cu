@@ -54,7 +54,8 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 // byte offsets of the sub-buffers inside the array
 constexpr size_t kOffFrame = 0;
 constexpr size_t kOffRtri = align256(kOffFrame + sizeof(FrameDesc));
-constexpr size_t kOffPoly = align256(kOffRtri + sizeof(RTri) * (size_t)kRtriCap);
+constexpr size_t kOffRtriZlo = kOffRtri + sizeof(RTri) * (size_t)kRtriCap;
+constexpr size_t kOffPoly = align256(kOffRtriZlo + 4 * (size_t)kRtriCap);
 constexpr size_t kOffClipList = align256(kOffPoly + sizeof(ClipPoly) * (size_t)kPolyCap);
 constexpr size_t kOffCount = align256(kOffClipList + 4 * (size_t)kPolyCap);
 constexpr size_t kOffOffset = align256(kOffCount + 4 * (size_t)(kMaxTiles + 1));
@@ -181,6 +182,7 @@ edxr_status edxr_render_noalloc(const edxr_mesh* mesh, const float mv[16], const
     a.total_tris = f.nt;
     a.total_tiles = tiles;
     a.rtris = reinterpret_cast<RTri*>(base + kOffRtri);
+    a.rtri_zlo = reinterpret_cast<uint32_t*>(base + kOffRtriZlo);
     a.rtri_capacity = kRtriCap;
     a.polys = reinterpret_cast<ClipPoly*>(base + kOffPoly);
     a.clip_list = reinterpret_cast<uint32_t*>(base + kOffClipList);
