@@ -1531,13 +1531,19 @@ __global__ void __launch_bounds__(kRasterThreads, MinBlocks) k_raster(PassArgs a
         bool split = (item.x & kSplitTile) != 0;
         // the item's range within the entries its bin kept (the scatter drops
         // entries hidden behind the tile's occluder)
-        const uint32_t kept = a.tile_cursor[tile], bin0 = a.tile_offset[tile];
-        const uint32_t e1 = min(item.z, bin0 + kept), e0 = min(item.y, e1);
-        if (split && e0 == e1)
+        uint32_t e0 = item.y, e1 = item.z, kept = 0;
+        if (e0 != e1)
         {
-            if (item.y != bin0 || kept != 0)
-                continue;  // the tile's kept entries are in its other items
-            split = false;  // it kept none: its first item writes the background
+            const uint32_t bin0 = a.tile_offset[tile];
+            kept = a.tile_cursor[tile];
+            e1 = min(e1, bin0 + kept);
+            e0 = min(e0, e1);
+            if (split && e0 == e1)
+            {
+                if (item.y != bin0 || kept != 0)
+                    continue;  // the tile's kept entries are in its other items
+                split = false;  // it kept none: its first item writes the background
+            }
         }
         if (e0 == e1 && !split)
         {
@@ -1913,13 +1919,19 @@ __global__ void __launch_bounds__(128, S <= 4 ? 5 : 3) k_raster_ms(const __grid_
         bool split = (item.x & kSplitTile) != 0;
         // the item's range within the entries its bin kept (the scatter drops
         // entries hidden behind the tile's occluder)
-        const uint32_t kept = a.tile_cursor[tile], bin0 = a.tile_offset[tile];
-        const uint32_t e1 = min(item.z, bin0 + kept), e0 = min(item.y, e1);
-        if (split && e0 == e1)
+        uint32_t e0 = item.y, e1 = item.z, kept = 0;
+        if (e0 != e1)
         {
-            if (item.y != bin0 || kept != 0)
-                continue;  // the tile's kept entries are in its other items
-            split = false;  // it kept none: its first item writes the background
+            const uint32_t bin0 = a.tile_offset[tile];
+            kept = a.tile_cursor[tile];
+            e1 = min(e1, bin0 + kept);
+            e0 = min(e0, e1);
+            if (split && e0 == e1)
+            {
+                if (item.y != bin0 || kept != 0)
+                    continue;  // the tile's kept entries are in its other items
+                split = false;  // it kept none: its first item writes the background
+            }
         }
         if (e0 == e1 && !split)
         {
