@@ -869,6 +869,7 @@ __global__ void __launch_bounds__(256, 4) k_bin_big(PassArgs a)
     };
     // batches of up to 32 triangles, small enough that every warp gets one
     const uint32_t batch = min(32u, max(1u, (nb + nw - 1) / nw));
+    const bool early_cull = nb >= a.total_tiles;
     for (uint32_t b0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * batch; b0 < nb; b0 += nw * batch)
     {
         // this lane's triangle of the batch and its number of 32x32 tiles
@@ -919,6 +920,20 @@ __global__ void __launch_bounds__(256, 4) k_bin_big(PassArgs a)
                 dq = quad_decisions(t, e, g, f, T32x, T32y);
                 tdx = f.tdx;
                 tile00 = f.tile_base + (uint32_t)(2 * T32y * f.tdx + 2 * T32x);
+                // a quadrant already hidden behind its tile's occluder bound
+                // (which only falls) gets no entry: the scatter would drop it.
+                // Checked when big triangles outnumber tiles (deep overdraw of
+                // large triangles); with few, the check's load costs more.
+                const uint32_t zlo = early_cull ? zmin_key(t, wrap_free(t)) : 0u;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (early_cull && ((dq >> (2 * q)) & 3u))
+                    {
+                        const uint32_t tq = tile00 + (uint32_t)((q >> 1) * tdx + (q & 1));
+                        const uint32_t zocc_now = *(volatile uint32_t*)&a.tile_zocc[tq];
+                        if (zocc_now != 0xFFFFFFFFu && zlo > min(zocc_now, 0xBF800000u))
+                            dq &= ~(3u << (2 * q));
+                    }
             }
             const uint32_t nz = (dq | (dq >> 1)) & 0x55u;
             const int cnt = __popc(nz);
